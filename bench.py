@@ -1,0 +1,284 @@
+"""Benchmark: output amplitudes per second of the 7x7 grid random circuit of
+depth (1+32+1) (49 qubits, CZ bond dimension 16), contracted with the
+two-cut 7x7 ordering (4 values per cut -> 16 slices summed per amplitude).
+
+One step = one call of the engine's public C-ABI entry
+qflex_gb300_evaluate_many for B random 49-bit output strings (host texts
+and strings in, complex128 amplitudes out). Every step uses new strings.
+
+  value  amplitudes/s from the engine's device time (flatten + program +
+         FP64 sums, CUDA events on the launching stream; inputs already in
+         HBM once the strings' bits are uploaded)
+  e2e    amplitudes/s of the whole C-ABI call (host->device bits, device->
+         host amplitudes, host planning cached) timed with CUDA events
+         around the K steps.
+
+Launch: python bench.py [--gpus N --steps K --warmup W --batch B]
+        python bench.py --impl reference ...   (reference's CPU path)
+Under torchrun each rank runs independent replicas on its own strings
+(the path shards over output strings; no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "amplitudes/s on 7x7 1+32+1 RQC; split-precision vs FP32, rel err≤1e-5 vs FP64"
+UNIT = "amplitudes/s"
+WORKLOAD = "c3"
+FP32_PEAK_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12  # TFLOP/s, FP32 CUDA-core FMA
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--batch", type=int, default=8, help="output strings per step")
+    p.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    p.add_argument("--precision", default="fp32")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_sample():
+    """The oracle port (numpy over OpenBLAS, the reference's algorithm) on
+    one cut slice of the benchmark workload x one output string. Returns
+    (seconds, amplitudes/s extrapolated by the planned flop ratio, sample
+    description, cores)."""
+    import numpy as np
+
+    from oracle import qflex_oracle as qo
+    from qflex_gb300 import Context, rqc
+    circuit, ordering, grid, initial, finals = rqc.workload(WORKLOAD)
+    one = rqc.ordering_7x7((0,), (1,))
+    plan = Context(-1)
+    plan.evaluate(circuit, ordering, grid, initial, finals[0], 1 << 40)
+    flop_full = plan.stats()["gemm_flop"]
+    plan.evaluate(circuit, one, grid, initial, finals[0], 1 << 40)
+    flop_one = plan.stats()["gemm_flop"]
+    inp = qo.Input(qo.Circuit.loads(circuit), qo.load_ordering(one), qo.Grid.loads(grid), initial, finals[0])
+    t0 = time.perf_counter()
+    qo.evaluate_circuit(inp, np.complex64, float(1 << 40))
+    dt = time.perf_counter() - t0
+    value = (flop_one / flop_full) / dt
+    desc = (f"one cut slice x 1 string of the 7x7 (1+32+1) workload ({flop_one:.3e} flop, {dt:.2f} s), "
+            f"scaled to the 16-slice amplitude ({flop_full:.3e} flop) by the flop ratio")
+    return dt, value, desc, os.cpu_count()
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    for _ in range(args.warmup):
+        cpu_sample()
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        dt, v, desc, cores = cpu_sample()
+        vals.append(v)
+    wall = time.perf_counter() - t0
+    value = statistics.mean(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+            "data": "synthetic", "config": config(args),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def config(args):
+    return {"workload": "7x7 grid RQC depth (1+32+1), 49 qubits, CZ bond 16, two cuts x 4 values "
+                        "(16 slices), random 49-bit output strings",
+            "strings_per_step": args.batch, "precision": args.precision,
+            "parallelism": f"replicas{args.gpus}",
+            "l2": "inputs larger than L2 (1.1 GB HBM arena per output string)"}
+
+
+def dominant_kernel_time(ctx, torch, m, n, k, reps=5):
+    """CUDA-event time of the dominant product shape on the context's stream."""
+    A = torch.randn((m, k), dtype=torch.complex64, device="cuda")
+    B = torch.randn((k, n), dtype=torch.complex64, device="cuda")
+    C = torch.empty((m, n), dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()
+    ctx.multiply(A.data_ptr(), B.data_ptr(), C.data_ptr(), m, n, k)
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        ctx.multiply(A.data_ptr(), B.data_ptr(), C.data_ptr(), m, n, k)
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    import torch
+    import torch.distributed as dist
+    from qflex_gb300 import Context, rqc
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    ctx = Context(local)
+    ctx.set_precision(args.precision)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    circuit, ordering, grid, initial, finals = rqc.workload(WORKLOAD)
+    B = args.batch
+
+    def strings(step):
+        # rank r takes its own strings; the 1024-string list is reused
+        # cyclically beyond 1024 / (world * B) steps.
+        base = ((step * world) + rank) * B
+        return [finals[(base + i) % len(finals)] for i in range(B)]
+
+    for w in range(args.warmup):
+        ctx.evaluate_many(circuit, ordering, grid, initial, strings(w), 1 << 40)
+    st = ctx.stats()
+    launches_per_step = int(st["n_ops"]) + 2
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    device_ms = 0.0
+    with ClockSampler(local) as clocks:
+        barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for s in range(args.steps):
+            ctx.evaluate_many(circuit, ordering, grid, initial, strings(args.warmup + s), 1 << 40)
+            device_ms += ctx.stats()["device_ms"]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([device_ms, e2e_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        device_ms, e2e_ms = t.tolist()
+    amps = args.steps * B * world
+    value = amps / (device_ms / 1000.0)
+    e2e = amps / (e2e_ms / 1000.0)
+
+    # Roofline of the dominant kernel (the 4096^3 complex product).
+    shapes = sorted(ctx.shapes(), key=lambda x: -x[0] * x[1] * x[2] * x[3])
+    m, n, k, _ = shapes[0]
+    kt_ms = dominant_kernel_time(ctx, torch, m, n, k)
+    achieved = 8.0 * m * n * k / (kt_ms / 1e3) / 1e12
+    roofline = {"bound": "fp32", "kernel": f"cgemm_fp32 ({m},{n},{k})", "achieved": achieved,
+                "peak": FP32_PEAK_NOMINAL, "unit": "TFLOP/s", "frac": achieved / FP32_PEAK_NOMINAL,
+                "peak_source": "nominal FP32 CUDA-core FMA rate (152 SMs x 128 lanes x 2 x 2.07 GHz); "
+                               "MEASURED_PEAKS.json has no FP32 CUDA-core figure",
+                "traffic": None, "timing": "CUDA events on the context stream, dominant shape, 5 launches"}
+    gflop = st["gemm_flop"]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": e2e_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+            "config": config(args),
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * 49 * B,
+                    "d2h_bytes_per_step": 16 * B},
+            "gpu_launches": launches_per_step * args.steps,
+            "algorithmic_tflops": gflop * B * args.steps * world / (device_ms / 1e3) / 1e12,
+            "roofline": roofline, "clocks": clocks.summary(),
+            "plan": {"gemm_flop_per_amplitude": gflop, "permute_bytes_per_amplitude": st["permute_bytes"],
+                     "arena_bytes_per_string": st["arena_bytes"], "ops": st["n_ops"],
+                     "slices": st["n_leaves"]}}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        dt, v, desc, cores = cpu_sample()
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

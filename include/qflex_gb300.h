@@ -1,0 +1,145 @@
+/*
+ * qflex_gb300 — C ABI of the GB300 engine for qFlex grid tensor-network
+ * contraction (random quantum circuit amplitudes).
+ *
+ * Plain pointers and sizes only; no exception crosses this boundary. Every
+ * function returns QFLEX_GB300_OK or an error code, and the message of the
+ * last failure is available from qflex_gb300_last_error(). Reference errors
+ * (bad circuit, grid or ordering text, memory limit, ...) carry the same
+ * message text as the reference's thrown std::string.
+ *
+ * One context = one CUDA device + one stream; a context must be used from
+ * one thread at a time (the reference itself is not thread-safe:
+ * src/tensor.cpp:83, src/global.h:9-15).
+ *
+ * Citations are paths inside the ngnrsaa/qflex project.
+ */
+#ifndef QFLEX_GB300_H
+#define QFLEX_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QFLEX_GB300_OK 0
+#define QFLEX_GB300_ERR_INPUT 1 /* the reference would throw std::string */
+#define QFLEX_GB300_ERR_CUDA 2  /* CUDA runtime failure */
+#define QFLEX_GB300_ERR_ARG 3   /* invalid argument to this API */
+
+/* Arithmetic of the complex64 contractions. */
+#define QFLEX_GB300_FP32 0   /* FP32 CUDA cores (matches complex<float>) */
+#define QFLEX_GB300_TF32X3 1 /* split 3xTF32 on tcgen05 tensor cores */
+#define QFLEX_GB300_BF16X3 2 /* split BF16x3 on tcgen05 tensor cores */
+
+typedef struct qflex_gb300_context qflex_gb300_context;
+
+typedef struct {
+  double device_ms;       /* device time of the last evaluation */
+  double gemm_flop;       /* 8*m*n*k summed over products, per final state */
+  double permute_bytes;   /* 16*size summed over permutes, per final state */
+  double arena_bytes;     /* HBM arena of one final state */
+  double reference_bytes; /* the reference's planned scratch (memory check) */
+  size_t n_ops;           /* device ops of the program */
+  size_t n_leaves;        /* contraction leaves (cut slices x terminal values) */
+  size_t batch;           /* final states evaluated per device pass */
+} qflex_gb300_stats;
+
+/* Creates a context on CUDA device `device`. No reference counterpart (the
+ * reference allocates per call inside ContractGrid,
+ * src/contraction_utils.cpp:612-639). device = -1 creates a planning-only
+ * context: evaluations parse, validate and plan (errors, output states,
+ * statistics, product shapes) without touching a GPU, and amplitudes are
+ * NaN. */
+int qflex_gb300_create(int device, int precision, qflex_gb300_context** out);
+void qflex_gb300_destroy(qflex_gb300_context* ctx);
+const char* qflex_gb300_last_error(const qflex_gb300_context* ctx);
+int qflex_gb300_set_precision(qflex_gb300_context* ctx, int precision);
+/* Runs all work of this context on `stream` (a cudaStream_t); NULL restores
+ * the context's own stream. */
+int qflex_gb300_set_stream(qflex_gb300_context* ctx, void* stream);
+
+/* Replaces qflex::EvaluateCircuit(QflexInput*)
+ * (src/evaluate_circuit.h:81-82, src/evaluate_circuit.cpp:106-253).
+ * `circuit`, `ordering`, `grid` are the texts of the three input files
+ * (formats of src/circuit.cpp:30-206, src/ordering.cpp:10-45,
+ * src/grid.cpp:11-45; docs/input_formats.md). `initial_state` and
+ * `final_state` may be empty, as in QflexInput (src/input.h:11-17).
+ * `memory_limit` in bytes plays the role of global::memory_limit
+ * (src/global.h:12); <= 0 means the reference default of 1 GiB.
+ * Results are kept in the context (see the accessors below). */
+int qflex_gb300_evaluate(qflex_gb300_context* ctx, const char* circuit, const char* ordering,
+                         const char* grid, const char* initial_state, const char* final_state,
+                         double memory_limit);
+
+/* The batched form: one contraction per final state, all of them run as one
+ * device batch. Each final state gives the amplitudes EvaluateCircuit would
+ * return for it; results are concatenated in input order. The reference has
+ * no batched call; its pybind layer rejects several final states
+ * (src/pybind_main.cpp:111-113), and callers loop instead
+ * (qflexcirq/interface/qflex_simulator.py:44-53). */
+int qflex_gb300_evaluate_many(qflex_gb300_context* ctx, const char* circuit, const char* ordering,
+                              const char* grid, const char* initial_state,
+                              const char* const* final_states, size_t n_final_states,
+                              double memory_limit);
+
+/* Results of the last evaluation: the (state, amplitude) pairs of
+ * src/evaluate_circuit.cpp:245-247, and the mutated initial/final states of
+ * QflexInput (src/evaluate_circuit.cpp:130-145). */
+size_t qflex_gb300_result_count(const qflex_gb300_context* ctx);
+const char* qflex_gb300_result_state(const qflex_gb300_context* ctx, size_t i);
+int qflex_gb300_result_amplitude(const qflex_gb300_context* ctx, size_t i, double* re, double* im);
+const char* qflex_gb300_result_initial_state(const qflex_gb300_context* ctx);
+/* Mutated final state of final state number `which` of the last call. */
+const char* qflex_gb300_result_final_state(const qflex_gb300_context* ctx, size_t which);
+int qflex_gb300_last_stats(const qflex_gb300_context* ctx, qflex_gb300_stats* out);
+/* Distinct product shapes of the last plan: writes up to `cap` rows of
+ * (m, n, k, count) into `out` and returns the number of distinct shapes. */
+size_t qflex_gb300_last_shapes(const qflex_gb300_context* ctx, size_t* out, size_t cap);
+/* Every product of the last plan in execution order: up to `cap` rows of
+ * (m, n, k). These are the (m, n, k) the reference passes to cblas_cgemm,
+ * cgemv and cdotu_sub inside ContractGrid (src/tensor.cpp:973-1041), in the
+ * same order. Returns the number of products. */
+size_t qflex_gb300_last_gemms(const qflex_gb300_context* ctx, size_t* out, size_t cap);
+
+/* ---- tensor-level operations on device memory (complex64, interleaved) ----
+ * Pointers are CUDA device pointers; work is queued on the context's stream.
+ */
+
+/* Out-of-place index permutation: the data movement of Tensor::reorder
+ * (src/tensor.cpp:866-911). The tensor has `rank` indices with dimensions
+ * `dims` (row-major, last index fastest, every dimension a power of two);
+ * `new_order[i]` is the old position of the index that goes to position i.
+ * `batch` tensors at a distance of `batch_stride` elements are permuted. */
+int qflex_gb300_permute(qflex_gb300_context* ctx, const void* src, void* dst, size_t rank,
+                        const size_t* dims, const size_t* new_order, size_t batch,
+                        size_t batch_stride);
+
+/* Host-side check of the permutation kernel's tiling: runs the kernel's
+ * exact index schedule (same tables, same tile order) over HOST buffers of
+ * complex64. For tests and diagnostics; needs no GPU and no context. No
+ * reference counterpart. */
+int qflex_gb300_check_permute(size_t rank, const size_t* dims, const size_t* new_order,
+                              const void* src_host, void* dst_host);
+
+/* In-place reorder with caller-provided scratch of at least the tensor's
+ * size: Tensor::reorder(new_ordering, scratch_copy) (src/tensor.h:215,
+ * src/tensor.cpp:866-911). Afterwards `data` holds the permuted tensor. */
+int qflex_gb300_reorder(qflex_gb300_context* ctx, void* data, void* scratch, size_t rank,
+                        const size_t* dims, const size_t* new_order);
+
+/* C[m,n] = A[m,k] * B[k,n], row-major complex64, alpha = 1, beta = 0: the
+ * products multiply() hands to cblas_cgemm / cgemv / cdotu_sub
+ * (src/tensor.cpp:960-1042). `batch` products at a distance of
+ * `batch_stride` elements. */
+int qflex_gb300_multiply(qflex_gb300_context* ctx, const void* A, const void* B, void* C, size_t m,
+                         size_t n, size_t k, size_t batch, size_t batch_stride);
+
+int qflex_gb300_synchronize(qflex_gb300_context* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QFLEX_GB300_H */

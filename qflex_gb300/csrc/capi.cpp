@@ -1,0 +1,298 @@
+// extern "C" boundary of the engine (declared in include/qflex_gb300.h).
+// Converts thrown std::string / std::exception into status codes.
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <new>
+
+#include "../../include/qflex_gb300.h"
+#include "engine.h"
+
+struct qflex_gb300_context {
+  std::unique_ptr<qfx::Engine> engine;
+  std::string error;
+  std::string initial;
+  std::vector<std::string> finals;
+  std::vector<std::string> states;
+  std::vector<std::complex<double>> amps;
+};
+
+namespace {
+
+constexpr double kDefaultMemoryLimit = double(1ull << 30);
+
+template <typename F>
+int guarded(qflex_gb300_context* ctx, F&& f) {
+  if (!ctx) return QFLEX_GB300_ERR_ARG;
+  try {
+    f();
+    ctx->error.clear();
+    return QFLEX_GB300_OK;
+  } catch (const std::string& e) {
+    ctx->error = e;
+    return e.rfind("ERROR (qflex_gb300: CUDA", 0) == 0 ? QFLEX_GB300_ERR_CUDA : QFLEX_GB300_ERR_INPUT;
+  } catch (const char* e) {
+    ctx->error = e;
+    return QFLEX_GB300_ERR_INPUT;
+  } catch (const std::bad_alloc&) {
+    ctx->error = "ERROR (qflex_gb300) --> host allocation failed";
+    return QFLEX_GB300_ERR_ARG;
+  } catch (const std::exception& e) {
+    ctx->error = e.what();
+    return QFLEX_GB300_ERR_INPUT;
+  }
+}
+
+void store(qflex_gb300_context* ctx, std::vector<qfx::EvalResult>&& res) {
+  ctx->states.clear();
+  ctx->amps.clear();
+  ctx->finals.clear();
+  ctx->initial = res.empty() ? std::string() : res[0].initial_state;
+  for (auto& r : res) {
+    ctx->finals.push_back(r.final_state);
+    for (std::size_t i = 0; i < r.states.size(); ++i) {
+      ctx->states.push_back(r.states[i]);
+      ctx->amps.push_back(r.amplitudes[i]);
+    }
+  }
+}
+
+void check_perm(std::size_t rank, const std::size_t* dims, const std::size_t* order, int* nbits,
+                std::uint8_t* perm) {
+  if (rank > 0 && (!dims || !order)) throw QFX_ERR("dims and new_order must be non-null.");
+  std::vector<int> lg(rank);
+  int total = 0;
+  std::vector<bool> seen(rank, false);
+  for (std::size_t i = 0; i < rank; ++i) {
+    int l = 0;
+    while ((std::size_t(1) << l) < dims[i]) ++l;
+    if ((std::size_t(1) << l) != dims[i]) throw QFX_ERR("Dimension ", dims[i], " is not a power of two.");
+    lg[i] = l;
+    total += l;
+    if (order[i] >= rank || seen[order[i]])
+      throw QFX_ERR("new_order must be a permutation of 0..", rank - 1, ".");
+    seen[order[i]] = true;
+  }
+  if (total > 31) throw QFX_ERR("Tensor of 2^", total, " elements is too large.");
+  std::vector<int> s_old(rank, 0), s_new(rank, 0), new_pos(rank);
+  for (std::size_t i = rank; i-- > 1;) s_old[i - 1] = s_old[i] + lg[i];
+  for (std::size_t p = 0; p < rank; ++p) new_pos[order[p]] = (int)p;
+  for (std::size_t p = rank; p-- > 1;) s_new[p - 1] = s_new[p] + lg[order[p]];
+  for (std::size_t i = 0; i < rank; ++i)
+    for (int b = 0; b < lg[i]; ++b) perm[s_old[i] + b] = (std::uint8_t)(s_new[new_pos[i]] + b);
+  *nbits = total;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qflex_gb300_create(int device, int precision, qflex_gb300_context** out) {
+  if (!out) return QFLEX_GB300_ERR_ARG;
+  *out = nullptr;
+  auto* ctx = new (std::nothrow) qflex_gb300_context();
+  if (!ctx) return QFLEX_GB300_ERR_ARG;
+  int rc = guarded(ctx, [&] { ctx->engine = std::make_unique<qfx::Engine>(device, precision); });
+  *out = ctx;  // returned even on failure so the error text can be read
+  return rc;
+}
+
+void qflex_gb300_destroy(qflex_gb300_context* ctx) { delete ctx; }
+
+const char* qflex_gb300_last_error(const qflex_gb300_context* ctx) {
+  return ctx ? ctx->error.c_str() : "null context";
+}
+
+int qflex_gb300_set_precision(qflex_gb300_context* ctx, int precision) {
+  return guarded(ctx, [&] {
+    if (!ctx->engine) throw QFX_ERR("context has no engine");
+    ctx->engine->set_precision(precision);
+  });
+}
+
+int qflex_gb300_set_stream(qflex_gb300_context* ctx, void* stream) {
+  return guarded(ctx, [&] {
+    if (!ctx->engine) throw QFX_ERR("context has no engine");
+    if (stream) {
+      ctx->engine->set_stream((cudaStream_t)stream);
+    } else {
+      cudaStream_t s;
+      cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+      if (e != cudaSuccess) throw qfx::cuda_error_string(e, "cudaStreamCreate");
+      ctx->engine->set_stream(s);
+    }
+  });
+}
+
+int qflex_gb300_evaluate(qflex_gb300_context* ctx, const char* circuit, const char* ordering,
+                         const char* grid, const char* initial_state, const char* final_state,
+                         double memory_limit) {
+  const char* finals[1] = {final_state ? final_state : ""};
+  return qflex_gb300_evaluate_many(ctx, circuit, ordering, grid, initial_state, finals, 1,
+                                   memory_limit);
+}
+
+int qflex_gb300_evaluate_many(qflex_gb300_context* ctx, const char* circuit, const char* ordering,
+                              const char* grid, const char* initial_state,
+                              const char* const* final_states, size_t n_final_states,
+                              double memory_limit) {
+  return guarded(ctx, [&] {
+    if (!ctx->engine) throw QFX_ERR("context has no engine");
+    if (!final_states && n_final_states) throw QFX_ERR("final_states must be non-null.");
+    std::vector<std::string> finals;
+    for (size_t i = 0; i < n_final_states; ++i) finals.emplace_back(final_states[i] ? final_states[i] : "");
+    const double limit = memory_limit > 0 ? memory_limit : kDefaultMemoryLimit;
+    store(ctx, ctx->engine->evaluate(circuit ? circuit : "", ordering ? ordering : "",
+                                     grid ? grid : "", initial_state ? initial_state : "", finals,
+                                     limit));
+  });
+}
+
+size_t qflex_gb300_result_count(const qflex_gb300_context* ctx) { return ctx ? ctx->amps.size() : 0; }
+
+const char* qflex_gb300_result_state(const qflex_gb300_context* ctx, size_t i) {
+  return (ctx && i < ctx->states.size()) ? ctx->states[i].c_str() : nullptr;
+}
+
+int qflex_gb300_result_amplitude(const qflex_gb300_context* ctx, size_t i, double* re, double* im) {
+  if (!ctx || i >= ctx->amps.size() || !re || !im) return QFLEX_GB300_ERR_ARG;
+  *re = ctx->amps[i].real();
+  *im = ctx->amps[i].imag();
+  return QFLEX_GB300_OK;
+}
+
+const char* qflex_gb300_result_initial_state(const qflex_gb300_context* ctx) {
+  return ctx ? ctx->initial.c_str() : nullptr;
+}
+
+const char* qflex_gb300_result_final_state(const qflex_gb300_context* ctx, size_t which) {
+  return (ctx && which < ctx->finals.size()) ? ctx->finals[which].c_str() : nullptr;
+}
+
+int qflex_gb300_last_stats(const qflex_gb300_context* ctx, qflex_gb300_stats* out) {
+  if (!ctx || !out || !ctx->engine) return QFLEX_GB300_ERR_ARG;
+  const auto& s = ctx->engine->last_stats();
+  out->device_ms = s.device_ms;
+  out->gemm_flop = s.gemm_flop;
+  out->permute_bytes = s.permute_bytes;
+  out->arena_bytes = double(s.arena_bytes);
+  out->reference_bytes = s.reference_bytes;
+  out->n_ops = s.n_ops;
+  out->n_leaves = s.n_leaves;
+  out->batch = s.batch;
+  return QFLEX_GB300_OK;
+}
+
+size_t qflex_gb300_last_shapes(const qflex_gb300_context* ctx, size_t* out, size_t cap) {
+  if (!ctx || !ctx->engine) return 0;
+  const auto& shapes = ctx->engine->last_shapes();
+  for (size_t i = 0; i < shapes.size() && i < cap && out; ++i) {
+    out[4 * i + 0] = shapes[i].m;
+    out[4 * i + 1] = shapes[i].n;
+    out[4 * i + 2] = shapes[i].k;
+    out[4 * i + 3] = shapes[i].count;
+  }
+  return shapes.size();
+}
+
+size_t qflex_gb300_last_gemms(const qflex_gb300_context* ctx, size_t* out, size_t cap) {
+  if (!ctx || !ctx->engine || !ctx->engine->last_program()) return 0;
+  size_t n = 0;
+  for (const auto& op : ctx->engine->last_program()->ops) {
+    if (op.kind != qfx::DevOp::GEMM) continue;
+    if (out && n < cap) {
+      out[3 * n + 0] = op.m;
+      out[3 * n + 1] = op.n;
+      out[3 * n + 2] = op.k;
+    }
+    ++n;
+  }
+  return n;
+}
+
+int qflex_gb300_permute(qflex_gb300_context* ctx, const void* src, void* dst, size_t rank,
+                        const size_t* dims, const size_t* new_order, size_t batch,
+                        size_t batch_stride) {
+  return guarded(ctx, [&] {
+    if (!ctx->engine) throw QFX_ERR("context has no engine");
+    if (!src || !dst) throw QFX_ERR("Data pointers must be non-null.");
+    if (src == dst) throw QFX_ERR("src and dst must not overlap; use qflex_gb300_reorder.");
+    if (batch == 0) return;
+    if (batch > 65535) throw QFX_ERR("batch must be at most 65535.");
+    int nbits = 0;
+    std::uint8_t perm[40] = {};
+    check_perm(rank, dims, new_order, &nbits, perm);
+    qfx::PermPlan plan;
+    qfx::make_perm_plan(nbits, perm, &plan);
+    cudaSetDevice(ctx->engine->device());
+    qfx::launch_permute(plan, (const float2*)src, (float2*)dst, batch_stride, (int)batch,
+                        ctx->engine->stream());
+  });
+}
+
+int qflex_gb300_check_permute(size_t rank, const size_t* dims, const size_t* new_order,
+                              const void* src_host, void* dst_host) {
+  try {
+    if (!src_host || !dst_host) return QFLEX_GB300_ERR_ARG;
+    int nbits = 0;
+    std::uint8_t perm[40] = {};
+    check_perm(rank, dims, new_order, &nbits, perm);
+    qfx::PermPlan plan;
+    qfx::make_perm_plan(nbits, perm, &plan);
+    qfx::permute_schedule_on_host(plan, (const float2*)src_host, (float2*)dst_host,
+                                  std::uint64_t(1) << nbits);
+    return QFLEX_GB300_OK;
+  } catch (...) {
+    return QFLEX_GB300_ERR_ARG;
+  }
+}
+
+int qflex_gb300_reorder(qflex_gb300_context* ctx, void* data, void* scratch, size_t rank,
+                        const size_t* dims, const size_t* new_order) {
+  return guarded(ctx, [&] {
+    if (!ctx->engine) throw QFX_ERR("context has no engine");
+    if (!scratch) throw QFX_ERR("Scratch copy must be non-null.");
+    if (!data) throw QFX_ERR("Data must be non-null.");
+    int nbits = 0;
+    std::uint8_t perm[40] = {};
+    check_perm(rank, dims, new_order, &nbits, perm);
+    bool identity = true;
+    for (int b = 0; b < nbits; ++b) identity &= perm[b] == b;
+    if (identity) return;
+    qfx::PermPlan plan;
+    qfx::make_perm_plan(nbits, perm, &plan);
+    cudaSetDevice(ctx->engine->device());
+    qfx::launch_permute(plan, (const float2*)data, (float2*)scratch, 0, 1, ctx->engine->stream());
+    cudaError_t e = cudaMemcpyAsync(data, scratch, (std::size_t(1) << nbits) * sizeof(float2),
+                                    cudaMemcpyDeviceToDevice, ctx->engine->stream());
+    if (e != cudaSuccess) throw qfx::cuda_error_string(e, "cudaMemcpyAsync");
+  });
+}
+
+int qflex_gb300_multiply(qflex_gb300_context* ctx, const void* A, const void* B, void* C, size_t m,
+                         size_t n, size_t k, size_t batch, size_t batch_stride) {
+  return guarded(ctx, [&] {
+    if (!ctx->engine) throw QFX_ERR("context has no engine");
+    if (!A) throw QFX_ERR("Data from Tensor A must be non-null.");
+    if (!B) throw QFX_ERR("Data from Tensor B must be non-null.");
+    if (!C) throw QFX_ERR("Data from Tensor C must be non-null.");
+    if (A == C) throw QFX_ERR("A and C cannot be the same tensor.");
+    if (B == C) throw QFX_ERR("B and C cannot be the same tensor.");
+    if (batch == 0 || m == 0 || n == 0) return;
+    if (batch > 65535) throw QFX_ERR("batch must be at most 65535.");
+    cudaSetDevice(ctx->engine->device());
+    qfx::launch_cgemm_fp32((const float2*)A, (const float2*)B, (float2*)C, m, n, k, batch_stride,
+                           (int)batch, ctx->engine->stream(), ctx->engine->skinny_scratch());
+  });
+}
+
+int qflex_gb300_synchronize(qflex_gb300_context* ctx) {
+  return guarded(ctx, [&] {
+    if (!ctx->engine) throw QFX_ERR("context has no engine");
+    cudaError_t e = cudaStreamSynchronize(ctx->engine->stream());
+    if (e != cudaSuccess) throw qfx::cuda_error_string(e, "cudaStreamSynchronize");
+  });
+}
+
+}  // extern "C"

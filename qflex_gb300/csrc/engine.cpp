@@ -1,0 +1,361 @@
+// EvaluateCircuit on the GPU (the flow of src/evaluate_circuit.cpp:106-253):
+// parse -> output states -> network description -> static program ->
+// one batched replay per group of final states.
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <unordered_map>
+
+namespace qfx {
+
+std::string cuda_error_string(cudaError_t e, const char* what) {
+  return cat("ERROR (qflex_gb300: CUDA ", what, ") --> ", cudaGetErrorString(e));
+}
+
+#define QFX_CUDA(call)                                                  \
+  do {                                                                  \
+    cudaError_t e_ = (call);                                            \
+    if (e_ != cudaSuccess) throw cuda_error_string(e_, #call);          \
+  } while (0)
+
+struct Engine::Plan {
+  std::string key;
+  Circuit circuit;
+  Grid grid;
+  Ordering ordering;
+  std::vector<Op> ops;
+  bool built = false;
+  Network net;
+  Program prog;
+  std::vector<PermPlan> perm;  // indexed like prog.ops (unused for GEMM ops)
+  std::uint32_t max_size_log2 = 0;
+  ColumnDesc* d_cols = nullptr;
+  StepDesc* d_steps = nullptr;
+  float2* d_mats = nullptr;
+  std::uint32_t* d_ptr = nullptr;
+  std::uint32_t* d_leaves = nullptr;
+  ~Plan() {
+    cudaFree(d_cols);
+    cudaFree(d_steps);
+    cudaFree(d_mats);
+    cudaFree(d_ptr);
+    cudaFree(d_leaves);
+  }
+};
+
+Engine::Engine(int device, int precision) : device_(device), precision_(precision) {
+  if (device < 0) {  // planning only: no CUDA calls at all
+    set_precision(precision);
+    return;
+  }
+  int n = 0;
+  QFX_CUDA(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) throw QFX_ERR("CUDA device ", device, " does not exist (", n, " visible).");
+  QFX_CUDA(cudaSetDevice(device_));
+  QFX_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  own_stream_ = true;
+  QFX_CUDA(cudaEventCreate(&ev0_));
+  QFX_CUDA(cudaEventCreate(&ev1_));
+  set_precision(precision);
+}
+
+Engine::~Engine() {
+  if (device_ < 0) return;
+  cudaSetDevice(device_);
+  if (stream_) cudaStreamSynchronize(stream_);
+  plan_.reset();
+  for (auto& b : bufs_) cudaFree(b.ptr);
+  if (ev0_) cudaEventDestroy(ev0_);
+  if (ev1_) cudaEventDestroy(ev1_);
+  if (own_stream_ && stream_) cudaStreamDestroy(stream_);
+}
+
+void Engine::set_precision(int p) {
+  if (p != FP32) throw QFX_ERR("Precision mode ", p, " is not available in this build.");
+  precision_ = p;
+}
+
+void Engine::set_stream(cudaStream_t s) {
+  if (own_stream_ && stream_) {
+    cudaStreamSynchronize(stream_);
+    cudaStreamDestroy(stream_);
+  }
+  own_stream_ = false;
+  stream_ = s;
+}
+
+void* Engine::reserve(std::size_t bytes, int slot) {
+  if ((int)bufs_.size() <= slot) bufs_.resize(slot + 1);
+  DevBuf& b = bufs_[slot];
+  if (b.bytes < bytes) {
+    QFX_CUDA(cudaStreamSynchronize(stream_));
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+    QFX_CUDA(cudaMalloc(&b.ptr, bytes));
+    b.bytes = bytes;
+  }
+  return b.ptr;
+}
+
+const std::vector<GemmShape>& Engine::last_shapes() const {
+  static const std::vector<GemmShape> none;
+  return plan_ && plan_->built ? plan_->prog.shapes : none;
+}
+
+const Program* Engine::last_program() const {
+  return plan_ && plan_->built ? &plan_->prog : nullptr;
+}
+
+Engine::Plan* Engine::get_plan(const std::string& circuit, const std::string& ordering,
+                               const std::string& grid) {
+  std::string key = circuit;
+  key += '\x01';
+  key += ordering;
+  key += '\x01';
+  key += grid;
+  if (plan_ && plan_->key == key) return plan_.get();
+  auto p = std::make_unique<Plan>();
+  p->key = std::move(key);
+  p->grid.load(grid);
+  p->circuit.load(circuit);
+  p->ordering.load(ordering);
+  p->ops = parse_ordering(p->ordering, p->grid);
+  plan_ = std::move(p);
+  return plan_.get();
+}
+
+namespace {
+
+// Flatten descriptors: where each column's 2D tensor lives and which bit of
+// its element index each two-qubit half reads.
+void build_flatten_tables(const Network& net, const Program& prog, std::vector<ColumnDesc>* cols,
+                          std::vector<StepDesc>* steps, std::vector<float2>* mats,
+                          std::uint32_t* max_log2) {
+  *max_log2 = 0;
+  for (std::size_t c = 0; c < net.columns.size(); ++c) {
+    const QubitColumn& col = net.columns[c];
+    const std::size_t r = col.indices.size();
+    std::vector<int> lg(r), start(r, 0);
+    int total = 0;
+    for (std::size_t i = 0; i < r; ++i) {
+      int l = 0;
+      while ((std::size_t(1) << l) < col.dims[i]) ++l;
+      lg[i] = l;
+      total += l;
+    }
+    for (std::size_t i = r; i-- > 1;) start[i - 1] = start[i] + lg[i];
+    ColumnDesc cd{};
+    cd.out_offset = prog.column_offset[c];
+    cd.size_log2 = (std::uint32_t)total;
+    cd.step_begin = (std::uint32_t)steps->size();
+    cd.o_shift = col.terminal ? start[0] : -1;
+    *max_log2 = std::max(*max_log2, cd.size_log2);
+    for (const ColumnStep& s : col.steps) {
+      StepDesc sd{};
+      sd.kind = (std::uint32_t)s.kind;
+      sd.V = (std::uint32_t)s.V;
+      sd.mat = (std::uint32_t)mats->size();
+      if (s.kind == 2) {
+        const Link& L = net.links[s.link];
+        auto it = std::find(col.indices.begin(), col.indices.end(), L.name);
+        if (it == col.indices.end()) throw QFX_ERR("Bond ", L.name, " is missing from its tensor.");
+        int shift = start[it - col.indices.begin()];
+        for (int u = s.ordinal + 1; u < L.n_gates; ++u) {
+          int l = 0;
+          while ((1 << l) < L.V[u]) ++l;
+          shift += l;
+        }
+        sd.shift = (std::uint32_t)shift;
+      }
+      for (const auto& z : s.data) mats->push_back(make_float2(z.real(), z.imag()));
+      steps->push_back(sd);
+    }
+    cd.step_end = (std::uint32_t)steps->size();
+    cols->push_back(cd);
+  }
+}
+
+template <typename T>
+T* upload(const std::vector<T>& v) {
+  T* d = nullptr;
+  const std::size_t bytes = std::max<std::size_t>(v.size(), 1) * sizeof(T);
+  QFX_CUDA(cudaMalloc(&d, bytes));
+  if (!v.empty()) QFX_CUDA(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return d;
+}
+
+}  // namespace
+
+void Engine::run_program(Plan& p, int batch, float2* arena) {
+  const Program& prog = p.prog;
+  const std::uint64_t stride = prog.arena_elems;
+  float2* scratch = skinny_scratch();
+  for (std::size_t i = 0; i < prog.ops.size(); ++i) {
+    const DevOp& op = prog.ops[i];
+    if (op.kind == DevOp::PERMUTE) {
+      launch_permute(p.perm[i], arena + op.a, arena + op.c, stride, batch, stream_);
+    } else {
+      launch_cgemm_fp32(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, batch,
+                        stream_, scratch);
+    }
+  }
+}
+
+float2* Engine::skinny_scratch() {
+  return (float2*)reserve(kSkinnyScratchElems * sizeof(float2), 3);
+}
+
+std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::string& ordering,
+                                         const std::string& grid, const std::string& initial_in,
+                                         const std::vector<std::string>& finals,
+                                         double memory_limit) {
+  if (device_ >= 0) QFX_CUDA(cudaSetDevice(device_));
+  if (finals.empty()) throw QFX_ERR("At least one final state is required.");
+  Plan& p = *get_plan(circuit, ordering, grid);
+  const long n_active = p.grid.I * p.grid.J - (long)p.grid.qubits_off.size();
+  std::string initial = initial_in.empty() ? std::string((std::size_t)std::max(0L, n_active), '0')
+                                           : initial_in;
+  std::vector<EvalResult> results(finals.size());
+  std::vector<Coord> final_qubits;
+  for (std::size_t f = 0; f < finals.size(); ++f) {
+    std::vector<Coord> fq;
+    std::vector<std::string> states;
+    std::string base;
+    try {
+      base = get_output_states(p.grid, p.ops, initial, finals[f], &fq, &states);
+    } catch (const std::string& e) {
+      throw QFX_WRAP("get_output_states", e);
+    }
+    results[f].initial_state = initial;
+    results[f].final_state = base;
+    results[f].states = std::move(states);
+    if (f == 0) final_qubits = fq;
+  }
+  if (!p.built) {
+    p.net = build_network(p.circuit, p.grid, initial, results[0].final_state, final_qubits, p.ops);
+    try {
+      p.prog = plan_contraction(p.net, p.ops, results[0].states.size(), INFINITY);
+    } catch (const std::string& e) {
+      throw QFX_WRAP("ContractGrid", e);
+    }
+    p.perm.resize(p.prog.ops.size());
+    for (std::size_t i = 0; i < p.prog.ops.size(); ++i)
+      if (p.prog.ops[i].kind == DevOp::PERMUTE)
+        make_perm_plan(p.prog.ops[i].nbits, p.prog.ops[i].perm, &p.perm[i]);
+    std::vector<ColumnDesc> cols;
+    std::vector<StepDesc> steps;
+    std::vector<float2> mats;
+    build_flatten_tables(p.net, p.prog, &cols, &steps, &mats, &p.max_size_log2);
+    std::vector<std::uint32_t> ptr(p.prog.n_amplitudes + 1, 0), leaves(p.prog.n_leaves);
+    for (std::size_t l = 0; l < p.prog.n_leaves; ++l) ++ptr[p.prog.leaf_amp[l] + 1];
+    for (std::size_t a = 0; a < p.prog.n_amplitudes; ++a) ptr[a + 1] += ptr[a];
+    std::vector<std::uint32_t> fill(ptr.begin(), ptr.end() - 1);
+    for (std::size_t l = 0; l < p.prog.n_leaves; ++l) leaves[fill[p.prog.leaf_amp[l]]++] = (std::uint32_t)l;
+    if (device_ >= 0) {
+      p.d_cols = upload(cols);
+      p.d_steps = upload(steps);
+      p.d_mats = upload(mats);
+      p.d_ptr = upload(ptr);
+      p.d_leaves = upload(leaves);
+    }
+    p.built = true;
+  } else {
+    if ((long)initial.size() != n_active)
+      throw QFX_ERR("Size of initial_conf: ", initial.size(),
+                    ", must be equal to the number of qubits: ", n_active, ".");
+  }
+  for (const auto& r : results)
+    if (r.final_state.size() != initial.size())
+      throw QFX_ERR("Size of final_conf: ", r.final_state.size(),
+                    ", must be equal to size of initial_conf: ", initial.size(), ".");
+  {
+    // The reference's memory-limit check (src/contraction_utils.cpp:147-155).
+    const double need = p.prog.reference_bytes;
+    if (need > memory_limit)
+      throw QFX_WRAP("ContractGrid",
+                     QFX_WRAP("Initialize", cat("Required space (", readable_memory_string(need),
+                                                ") exceeds memory limit (",
+                                                readable_memory_string(memory_limit),
+                                                "). Cancelling simulation.")));
+  }
+
+  const Program& prog = p.prog;
+  const std::size_t n_cols = p.net.columns.size();
+  const std::size_t n_amps = prog.n_amplitudes;
+  const std::size_t arena_bytes = prog.arena_elems * sizeof(float2);
+  const int total = (int)finals.size();
+
+  stats_ = RunStats{};
+  stats_.gemm_flop = prog.gemm_flop;
+  stats_.permute_bytes = prog.permute_bytes;
+  stats_.arena_bytes = arena_bytes;
+  stats_.n_ops = prog.ops.size();
+  stats_.n_leaves = prog.n_leaves;
+  stats_.reference_bytes = prog.reference_bytes;
+  if (device_ < 0) {  // planning-only context: amplitudes are not computed
+    for (auto& r : results) r.amplitudes.assign(n_amps, {NAN, NAN});
+    return results;
+  }
+
+  // How many final states fit on the device at once.
+  std::size_t free_b = 0, total_b = 0;
+  QFX_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const std::size_t have = bufs_.size() > 0 ? bufs_[0].bytes : 0;
+  const std::size_t usable = free_b + have > (std::size_t(2) << 30) ? free_b + have - (std::size_t(2) << 30) : 0;
+  int chunk = (int)std::max<std::size_t>(1, std::min<std::size_t>((std::size_t)total, usable / std::max<std::size_t>(arena_bytes, 1)));
+  chunk = std::min(chunk, 65535);
+
+  float2* arena = (float2*)reserve(arena_bytes * (std::size_t)chunk, 0);
+  double2* d_amps = (double2*)reserve(std::max<std::size_t>(n_amps, 1) * sizeof(double2) * (std::size_t)chunk, 1);
+  std::uint8_t* d_bits = (std::uint8_t*)reserve(std::max<std::size_t>(n_cols, 1) * 2 * (std::size_t)chunk, 2);
+
+  std::vector<std::uint8_t> init_bits(n_cols), bits;
+  for (std::size_t c = 0; c < n_cols; ++c) {
+    // Active qubits are numbered in row-major order, skipping off qubits.
+    init_bits[c] = initial[c] == '0' ? 0 : 1;
+  }
+  std::vector<double2> h_amps(std::max<std::size_t>(n_amps, 1) * (std::size_t)chunk);
+  double ms_total = 0;
+  for (int f0 = 0; f0 < total; f0 += chunk) {
+    const int nb = std::min(chunk, total - f0);
+    bits.assign(n_cols * 2 * (std::size_t)nb, 0);
+    for (int b = 0; b < nb; ++b) {
+      const std::string& fs = results[f0 + b].final_state;
+      for (std::size_t c = 0; c < n_cols; ++c) {
+        bits[(std::size_t)b * n_cols + c] = init_bits[c];
+        bits[(std::size_t)(nb + b) * n_cols + c] = fs[c] == '0' ? 0 : 1;
+      }
+    }
+    QFX_CUDA(cudaMemcpyAsync(d_bits, bits.data(), bits.size(), cudaMemcpyHostToDevice, stream_));
+    QFX_CUDA(cudaMemsetAsync(d_amps, 0, std::max<std::size_t>(n_amps, 1) * sizeof(double2) * nb, stream_));
+    QFX_CUDA(cudaEventRecord(ev0_, stream_));
+    launch_flatten(p.d_cols, (int)n_cols, p.max_size_log2, p.d_steps, p.d_mats, d_bits,
+                   d_bits + n_cols * (std::size_t)nb, arena, prog.arena_elems, nb, stream_);
+    run_program(p, nb, arena);
+    launch_reduce_amplitudes(arena + prog.results_offset, prog.arena_elems, p.d_ptr, p.d_leaves,
+                             (int)n_amps, d_amps, nb, stream_);
+    QFX_CUDA(cudaEventRecord(ev1_, stream_));
+    QFX_CUDA(cudaMemcpyAsync(h_amps.data(), d_amps, n_amps * sizeof(double2) * nb,
+                             cudaMemcpyDeviceToHost, stream_));
+    QFX_CUDA(cudaStreamSynchronize(stream_));
+    float ms = 0;
+    QFX_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
+    ms_total += ms;
+    for (int b = 0; b < nb; ++b) {
+      auto& r = results[f0 + b];
+      r.amplitudes.resize(n_amps);
+      for (std::size_t a = 0; a < n_amps; ++a) {
+        const double2 v = h_amps[(std::size_t)b * n_amps + a];
+        r.amplitudes[a] = {v.x, v.y};
+      }
+    }
+  }
+  stats_.device_ms = ms_total;
+  stats_.batch = (std::size_t)chunk;
+  return results;
+}
+
+}  // namespace qfx

@@ -1,0 +1,89 @@
+// The contraction engine: one CUDA device, one stream, a planned HBM arena.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <complex>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "planner.h"
+#include "qfx.h"
+
+namespace qfx {
+
+enum Precision : int { FP32 = 0, TF32X3 = 1, BF16X3 = 2 };
+
+struct EvalResult {
+  std::string initial_state;  // as mutated by EvaluateCircuit
+  std::string final_state;
+  std::vector<std::string> states;
+  std::vector<std::complex<double>> amplitudes;
+};
+
+struct RunStats {
+  double device_ms = 0;       // flatten + program + sums, CUDA events
+  double gemm_flop = 0;       // per final state
+  double permute_bytes = 0;   // per final state
+  std::size_t arena_bytes = 0;  // per final state
+  std::size_t n_ops = 0;
+  std::size_t n_leaves = 0;
+  std::size_t batch = 0;
+  double reference_bytes = 0;
+};
+
+class Engine {
+ public:
+  Engine(int device, int precision);
+  ~Engine();
+  Engine(const Engine&) = delete;
+  Engine& operator=(const Engine&) = delete;
+
+  void set_precision(int p);
+  int precision() const { return precision_; }
+  void set_stream(cudaStream_t s);
+  cudaStream_t stream() const { return stream_; }
+  int device() const { return device_; }
+
+  // EvaluateCircuit for one initial state and several final states (each
+  // one is a separate contraction of the same network; all of them run as
+  // one batch). Throws std::string on the reference's errors.
+  std::vector<EvalResult> evaluate(const std::string& circuit, const std::string& ordering,
+                                   const std::string& grid, const std::string& initial,
+                                   const std::vector<std::string>& finals, double memory_limit);
+
+  const RunStats& last_stats() const { return stats_; }
+  // Distinct GEMM shapes of the last plan (m, n, k, count).
+  const std::vector<GemmShape>& last_shapes() const;
+  // The last planned program (null before the first evaluation).
+  const Program* last_program() const;
+
+  // Device buffers owned by the engine, reused across calls.
+  void* reserve(std::size_t bytes, int slot);
+  // Partial-sum buffer of the split-k skinny products (kSkinnyScratchElems).
+  float2* skinny_scratch();
+
+ private:
+  struct Plan;
+  Plan* get_plan(const std::string& circuit, const std::string& ordering, const std::string& grid);
+  void run_program(Plan& p, int batch, float2* arena);
+
+  int device_;
+  int precision_;
+  cudaStream_t stream_ = nullptr;
+  bool own_stream_ = false;
+  std::unique_ptr<Plan> plan_;
+  struct DevBuf {
+    void* ptr = nullptr;
+    std::size_t bytes = 0;
+  };
+  std::vector<DevBuf> bufs_;
+  RunStats stats_;
+  cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+};
+
+std::string cuda_error_string(cudaError_t e, const char* what);
+
+}  // namespace qfx

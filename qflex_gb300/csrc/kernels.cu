@@ -1,0 +1,523 @@
+// sm_103a kernels of the contraction path: column flatten, binary-digit
+// permutation, complex64 products on CUDA cores, FP64 amplitude sums.
+#include <algorithm>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+
+namespace qfx {
+
+namespace {
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {
+  c.x = fmaf(a.x, b.x, c.x);
+  c.x = fmaf(-a.y, b.y, c.x);
+  c.y = fmaf(a.x, b.y, c.y);
+  c.y = fmaf(a.y, b.x, c.y);
+  return c;
+}
+
+void check_launch(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw std::string("ERROR (qflex_gb300: launch ") + what + ") --> " + cudaGetErrorString(e);
+}
+
+// ---------------------------------------------------------------------------
+// Column flatten.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) flatten_kernel(const ColumnDesc* __restrict__ cols,
+                                                      const StepDesc* __restrict__ steps,
+                                                      const float2* __restrict__ mats,
+                                                      const std::uint8_t* __restrict__ init_bits,
+                                                      const std::uint8_t* __restrict__ final_bits,
+                                                      int n_cols, float2* __restrict__ arena,
+                                                      std::uint64_t arena_stride) {
+  const int c = blockIdx.y;
+  const int b = blockIdx.z;
+  const ColumnDesc cd = cols[c];
+  const std::uint64_t e = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= (std::uint64_t(1) << cd.size_log2)) return;
+  float2 p0 = make_float2(1.f, 0.f), p1 = make_float2(0.f, 0.f);
+  if (init_bits[std::size_t(b) * n_cols + c]) {
+    p0 = make_float2(0.f, 0.f);
+    p1 = make_float2(1.f, 0.f);
+  }
+  for (std::uint32_t s = cd.step_begin; s < cd.step_end; ++s) {
+    const StepDesc sd = steps[s];
+    const float2* g = mats + sd.mat;
+    std::uint32_t row = 2;  // distance between input rows of the gate data
+    if (sd.kind == 2) {
+      const std::uint32_t v = std::uint32_t(e >> sd.shift) & (sd.V - 1);
+      g += 2 * v;
+      row = 2 * sd.V;
+    }
+    const float2 q0 = cfma(p1, __ldg(g + row), cmul(p0, __ldg(g)));
+    const float2 q1 = cfma(p1, __ldg(g + row + 1), cmul(p0, __ldg(g + 1)));
+    p0 = q0;
+    p1 = q1;
+  }
+  int bit;
+  if (cd.o_shift >= 0)
+    bit = int((e >> cd.o_shift) & 1);
+  else
+    bit = final_bits[std::size_t(b) * n_cols + c];
+  arena[std::uint64_t(b) * arena_stride + cd.out_offset + e] = bit ? p1 : p0;
+}
+
+// ---------------------------------------------------------------------------
+// Binary-digit permutation.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) permute_kernel(const __grid_constant__ PermPlan P,
+                                                      const float2* __restrict__ src,
+                                                      float2* __restrict__ dst,
+                                                      std::uint64_t batch_stride) {
+  __shared__ float2 tile[1024];
+  __shared__ std::uint32_t tab[6 * 32];
+  if (threadIdx.x < 6 * 32) tab[threadIdx.x] = P.tab[threadIdx.x / 32][threadIdx.x % 32];
+  __syncthreads();
+  const std::uint32_t T = 1u << P.tile_bits;
+  const float2* s = src + std::uint64_t(blockIdx.y) * batch_stride;
+  float2* d = dst + std::uint64_t(blockIdx.y) * batch_stride;
+  for (std::uint64_t t = blockIdx.x; t < P.n_tiles; t += gridDim.x) {
+    std::uint64_t bi, bo;
+    perm_tile_base(P, t, &bi, &bo);
+#pragma unroll 4
+    for (std::uint32_t j = threadIdx.x; j < T; j += blockDim.x)
+      tile[perm_swizzle(j)] = s[bi + tab[j & 31] + tab[32 + (j >> 5)]];
+    __syncthreads();
+#pragma unroll 4
+    for (std::uint32_t j = threadIdx.x; j < T; j += blockDim.x)
+      d[bo + tab[64 + (j & 31)] + tab[96 + (j >> 5)]] =
+          tile[perm_swizzle(tab[128 + (j & 31)] + tab[160 + (j >> 5)])];
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Complex64 GEMM on CUDA cores (C = A * B, row-major).
+// Block tile BM x BN, k-step BK; each thread owns a TM x TN sub-tile.
+// Operands pass through shared memory with a register-staged prefetch of
+// the next k-step.
+// ---------------------------------------------------------------------------
+template <int BM, int BN, int BK, int TM, int TN>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+    cgemm_kernel(const float2* __restrict__ A, const float2* __restrict__ B, float2* __restrict__ C,
+                 int m, int n, int k, std::uint64_t batch_stride) {
+  constexpr int NT = (BM / TM) * (BN / TN);
+  constexpr int TX = BN / TN;
+  constexpr int LA = BM * BK / NT;
+  constexpr int LB = BK * BN / NT;
+  static_assert(LA * NT == BM * BK && LB * NT == BK * BN, "tile/threads mismatch");
+  __shared__ __align__(16) float2 As[BK][BM + 2];
+  __shared__ __align__(16) float2 Bs[BK][BN + 2];
+
+  const std::uint64_t boff = std::uint64_t(blockIdx.z) * batch_stride;
+  A += boff;
+  B += boff;
+  C += boff;
+  const int tiles_m = (m + BM - 1) / BM;
+  const int m0 = int(blockIdx.x % tiles_m) * BM;
+  const int n0 = int(blockIdx.x / tiles_m) * BN;
+  const int t = threadIdx.x;
+  const int tx = t % TX, ty = t / TX;
+
+  float2 acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = make_float2(0.f, 0.f);
+
+  float2 ra[LA], rb[LB];
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int i = 0; i < LA; ++i) {
+      const int idx = t + i * NT;
+      const int r = idx / BK, c = idx % BK;
+      const int gr = m0 + r, gc = k0 + c;
+      ra[i] = (gr < m && gc < k) ? A[std::size_t(gr) * k + gc] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int i = 0; i < LB; ++i) {
+      const int idx = t + i * NT;
+      const int r = idx / BN, c = idx % BN;
+      const int gr = k0 + r, gc = n0 + c;
+      rb[i] = (gr < k && gc < n) ? B[std::size_t(gr) * n + gc] : make_float2(0.f, 0.f);
+    }
+  };
+  auto store = [&]() {
+#pragma unroll
+    for (int i = 0; i < LA; ++i) {
+      const int idx = t + i * NT;
+      As[idx % BK][idx / BK] = ra[i];
+    }
+#pragma unroll
+    for (int i = 0; i < LB; ++i) {
+      const int idx = t + i * NT;
+      Bs[idx / BN][idx % BN] = rb[i];
+    }
+  };
+
+  const int ktiles = (k + BK - 1) / BK;
+  load(0);
+  store();
+  __syncthreads();
+  for (int kt = 0; kt < ktiles; ++kt) {
+    const bool more = kt + 1 < ktiles;
+    if (more) load((kt + 1) * BK);
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      float2 a[TM], b[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = As[kk][ty * TM + i];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) b[j] = Bs[kk][tx * TN + j];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = cfma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+    if (more) {
+      store();
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    const int gr = m0 + ty * TM + i;
+    if (gr >= m) continue;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int gc = n0 + tx * TN + j;
+      if (gc < n) C[std::size_t(gr) * n + gc] = acc[i][j];
+    }
+  }
+}
+
+__device__ __forceinline__ float2 warp_sum(float2 v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+  }
+  return v;
+}
+
+// C[i] = sum_kk A[i, kk] * B[kk]; one thread per row (short rows).
+__global__ void __launch_bounds__(256) gemv_rows_thread(const float2* __restrict__ A,
+                                                        const float2* __restrict__ B,
+                                                        float2* __restrict__ C, std::uint64_t m,
+                                                        int k, std::uint64_t batch_stride) {
+  const std::uint64_t boff = std::uint64_t(blockIdx.y) * batch_stride;
+  const std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const float2* a = A + boff + i * k;
+  const float2* b = B + boff;
+  float2 acc = make_float2(0.f, 0.f);
+  for (int kk = 0; kk < k; ++kk) acc = cfma(a[kk], b[kk], acc);
+  C[boff + i] = acc;
+}
+
+// Same, one warp per row (long rows).
+__global__ void __launch_bounds__(256) gemv_rows_warp(const float2* __restrict__ A,
+                                                      const float2* __restrict__ B,
+                                                      float2* __restrict__ C, std::uint64_t m,
+                                                      std::uint64_t k, std::uint64_t batch_stride) {
+  const std::uint64_t boff = std::uint64_t(blockIdx.y) * batch_stride;
+  const std::uint64_t i = (std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
+  if (i >= m) return;
+  const float2* a = A + boff + i * k;
+  const float2* b = B + boff;
+  float2 acc = make_float2(0.f, 0.f);
+  for (std::uint64_t kk = lane; kk < k; kk += 32) acc = cfma(a[kk], b[kk], acc);
+  acc = warp_sum(acc);
+  if (lane == 0) C[boff + i] = acc;
+}
+
+// C[j] = sum_kk A[kk] * B[kk, j]; one thread per column (wide rows of B).
+__global__ void __launch_bounds__(256) gemv_cols_thread(const float2* __restrict__ A,
+                                                        const float2* __restrict__ B,
+                                                        float2* __restrict__ C, std::uint64_t n,
+                                                        std::uint64_t k, std::uint64_t batch_stride) {
+  const std::uint64_t boff = std::uint64_t(blockIdx.y) * batch_stride;
+  const std::uint64_t j = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const float2* a = A + boff;
+  const float2* b = B + boff + j;
+  float2 acc = make_float2(0.f, 0.f);
+  for (std::uint64_t kk = 0; kk < k; ++kk) acc = cfma(a[kk], b[kk * n], acc);
+  C[boff + j] = acc;
+}
+
+// Same, one block per column with a block-wide reduction (narrow B).
+__global__ void __launch_bounds__(256) gemv_cols_block(const float2* __restrict__ A,
+                                                       const float2* __restrict__ B,
+                                                       float2* __restrict__ C, std::uint64_t n,
+                                                       std::uint64_t k, std::uint64_t batch_stride) {
+  __shared__ float2 part[8];
+  const std::uint64_t boff = std::uint64_t(blockIdx.y) * batch_stride;
+  const std::uint64_t j = blockIdx.x;
+  const float2* a = A + boff;
+  const float2* b = B + boff + j;
+  float2 acc = make_float2(0.f, 0.f);
+  for (std::uint64_t kk = threadIdx.x; kk < k; kk += blockDim.x) acc = cfma(a[kk], b[kk * n], acc);
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x / 32] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float2 v = threadIdx.x < 8 ? part[threadIdx.x] : make_float2(0.f, 0.f);
+    v = warp_sum(v);
+    if (threadIdx.x == 0) C[boff + j] = v;
+  }
+}
+
+// Skinny products with a long contraction (m * n small, k large): the k range
+// is split over `splits` blocks per output; block (r, s) writes the FP32
+// partial sum of chunk s of output r, and skinny_finish adds the partials of
+// each output in chunk order (FP64), so the result does not depend on
+// scheduling.
+__global__ void __launch_bounds__(256) skinny_partial(const float2* __restrict__ A,
+                                                      const float2* __restrict__ B,
+                                                      float2* __restrict__ partial, int n,
+                                                      std::uint64_t k, int splits,
+                                                      std::uint64_t batch_stride) {
+  __shared__ float2 part[8];
+  const int r = blockIdx.x / splits, s = blockIdx.x % splits;
+  const int i = r / n, j = r % n;
+  const std::uint64_t boff = std::uint64_t(blockIdx.y) * batch_stride;
+  const std::uint64_t chunk = (k + splits - 1) / splits;
+  const std::uint64_t k0 = std::uint64_t(s) * chunk;
+  const std::uint64_t k1 = k0 + chunk < k ? k0 + chunk : k;
+  const float2* a = A + boff + std::uint64_t(i) * k;
+  const float2* b = B + boff + j;
+  float2 acc = make_float2(0.f, 0.f);
+  for (std::uint64_t kk = k0 + threadIdx.x; kk < k1; kk += blockDim.x) acc = cfma(a[kk], b[kk * n], acc);
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x / 32] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float2 v = threadIdx.x < 8 ? part[threadIdx.x] : make_float2(0.f, 0.f);
+    v = warp_sum(v);
+    if (threadIdx.x == 0) partial[(std::uint64_t(blockIdx.y) * gridDim.x) + blockIdx.x] = v;
+  }
+}
+
+__global__ void skinny_finish(const float2* __restrict__ partial, float2* __restrict__ C, int outputs,
+                              int splits, std::uint64_t batch_stride) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= outputs) return;
+  const float2* p = partial + (std::uint64_t(blockIdx.y) * outputs + r) * splits;
+  double re = 0, im = 0;
+  for (int s = 0; s < splits; ++s) {
+    re += double(p[s].x);
+    im += double(p[s].y);
+  }
+  C[std::uint64_t(blockIdx.y) * batch_stride + r] = make_float2(float(re), float(im));
+}
+
+__global__ void reduce_amplitudes_kernel(const float2* __restrict__ results, std::uint64_t stride,
+                                         const std::uint32_t* __restrict__ ptr,
+                                         const std::uint32_t* __restrict__ leaves, int n_amps,
+                                         double2* __restrict__ amps) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (a >= n_amps) return;
+  double re = 0, im = 0;
+  const float2* r = results + std::uint64_t(b) * stride;
+  for (std::uint32_t p = ptr[a]; p < ptr[a + 1]; ++p) {
+    const float2 v = r[leaves[p]];
+    re += double(v.x);
+    im += double(v.y);
+  }
+  double2& out = amps[std::size_t(b) * n_amps + a];
+  out.x += re;
+  out.y += im;
+}
+
+template <int BM, int BN, int BK, int TM, int TN>
+void run_cgemm(const float2* A, const float2* B, float2* C, std::size_t m, std::size_t n,
+               std::size_t k, std::uint64_t stride, int batch, cudaStream_t s) {
+  const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
+  dim3 grid((unsigned)tiles, 1, (unsigned)batch);
+  cgemm_kernel<BM, BN, BK, TM, TN><<<grid, (BM / TM) * (BN / TN), 0, s>>>(A, B, C, (int)m, (int)n,
+                                                                         (int)k, stride);
+  check_launch("cgemm");
+}
+
+}  // namespace
+
+void launch_flatten(const ColumnDesc* cols, int n_cols, std::uint32_t max_size_log2,
+                    const StepDesc* steps, const float2* mats, const std::uint8_t* init_bits,
+                    const std::uint8_t* final_bits, float2* arena, std::uint64_t arena_stride,
+                    int batch, cudaStream_t s) {
+  if (n_cols == 0) return;
+  const std::uint64_t blocks = ((std::uint64_t(1) << max_size_log2) + 255) / 256;
+  dim3 grid((unsigned)blocks, (unsigned)n_cols, (unsigned)batch);
+  flatten_kernel<<<grid, 256, 0, s>>>(cols, steps, mats, init_bits, final_bits, n_cols, arena,
+                                      arena_stride);
+  check_launch("flatten");
+}
+
+void make_perm_plan(int R, const std::uint8_t* perm, PermPlan* P) {
+  if (R > 31) throw std::string("ERROR (qflex_gb300: permute) --> tensor exceeds 2^31 elements");
+  std::memset(P, 0, sizeof(*P));
+  bool in_tile[40] = {};
+  const int want = std::min(10, R);
+  int a = std::min(5, R), c = std::min(5, R), count = 0;
+  auto recount = [&]() {
+    count = 0;
+    for (int p = 0; p < R; ++p) {
+      in_tile[p] = (p < a) || (perm[p] < c);
+      count += in_tile[p];
+    }
+  };
+  recount();
+  bool grow_in = true;
+  while (count < want) {
+    if ((grow_in && a < R) || c >= R)
+      ++a;
+    else
+      ++c;
+    grow_in = !grow_in;
+    recount();
+  }
+  int t_in[40], t_out[40], rank_in[40] = {};
+  int nt = 0;
+  for (int p = 0; p < R; ++p)
+    if (in_tile[p]) {
+      rank_in[p] = nt;
+      t_in[nt++] = p;
+    }
+  int no = 0;
+  for (int q = 0; q < R; ++q)  // tile digits ordered by output position
+    for (int p = 0; p < R; ++p)
+      if (in_tile[p] && perm[p] == q) t_out[no++] = p;
+  P->tile_bits = (std::uint32_t)nt;
+  int n_outer = 0;
+  for (int p = 0; p < R; ++p)
+    if (!in_tile[p]) {
+      P->outer_in[n_outer] = (std::uint8_t)p;
+      P->outer_out[n_outer] = perm[p];
+      ++n_outer;
+    }
+  P->n_outer = (std::uint32_t)n_outer;
+  P->n_tiles = std::uint64_t(1) << n_outer;
+  for (std::uint32_t j = 0; j < 32; ++j) {
+    for (int q = 0; q < 5; ++q) {
+      if (!((j >> q) & 1)) continue;
+      if (q < nt) {
+        P->tab[0][j] |= 1u << t_in[q];
+        P->tab[2][j] |= 1u << perm[t_out[q]];
+        P->tab[4][j] |= 1u << rank_in[t_out[q]];
+      }
+      if (q + 5 < nt) {
+        P->tab[1][j] |= 1u << t_in[q + 5];
+        P->tab[3][j] |= 1u << perm[t_out[q + 5]];
+        P->tab[5][j] |= 1u << rank_in[t_out[q + 5]];
+      }
+    }
+  }
+}
+
+void permute_schedule_on_host(const PermPlan& P, const float2* src, float2* dst,
+                              std::uint64_t size) {
+  std::vector<float2> tile(1024);
+  const std::uint32_t T = 1u << P.tile_bits;
+  for (std::uint64_t t = 0; t < P.n_tiles; ++t) {
+    std::uint64_t bi, bo;
+    perm_tile_base(P, t, &bi, &bo);
+    for (std::uint32_t j = 0; j < T; ++j) {
+      const std::uint32_t slot = perm_swizzle(j);
+      if (slot >= 1024) throw std::string("ERROR (qflex_gb300: permute) --> tile slot out of range");
+      const std::uint64_t at = bi + P.tab[0][j & 31] + P.tab[1][j >> 5];
+      if (at >= size) throw std::string("ERROR (qflex_gb300: permute) --> load out of range");
+      tile[slot] = src[at];
+    }
+    for (std::uint32_t j = 0; j < T; ++j) {
+      const std::uint32_t slot = perm_swizzle(P.tab[4][j & 31] + P.tab[5][j >> 5]);
+      if (slot >= T) throw std::string("ERROR (qflex_gb300: permute) --> tile slot out of range");
+      const std::uint64_t at = bo + P.tab[2][j & 31] + P.tab[3][j >> 5];
+      if (at >= size) throw std::string("ERROR (qflex_gb300: permute) --> store out of range");
+      dst[at] = tile[slot];
+    }
+  }
+}
+
+void launch_permute(const PermPlan& plan, const float2* src, float2* dst, std::uint64_t batch_stride,
+                    int batch, cudaStream_t s) {
+  const std::uint64_t tiles = plan.n_tiles;
+  const unsigned gx = (unsigned)std::min<std::uint64_t>(tiles, 152ull * 16ull);
+  dim3 grid(gx, (unsigned)batch, 1);
+  permute_kernel<<<grid, 256, 0, s>>>(plan, src, dst, batch_stride);
+  check_launch("permute");
+}
+
+int skinny_splits(std::size_t m, std::size_t n, std::size_t k, int batch) {
+  if (m * n > 64 || k < 8192) return 0;
+  std::size_t splits = std::min<std::size_t>(2048, (k + 4095) / 4096);
+  while (splits > 1 && splits * m * n * (std::size_t)batch > kSkinnyScratchElems) splits /= 2;
+  return splits >= 2 ? (int)splits : 0;
+}
+
+void launch_cgemm_fp32(const float2* A, const float2* B, float2* C, std::size_t m, std::size_t n,
+                       std::size_t k, std::uint64_t stride, int batch, cudaStream_t s,
+                       float2* scratch) {
+  if (const int splits = scratch ? skinny_splits(m, n, k, batch) : 0) {
+    const int outputs = (int)(m * n);
+    dim3 g1((unsigned)(outputs * splits), (unsigned)batch);
+    skinny_partial<<<g1, 256, 0, s>>>(A, B, scratch, (int)n, k, splits, stride);
+    check_launch("skinny_partial");
+    dim3 g2((unsigned)((outputs + 63) / 64), (unsigned)batch);
+    skinny_finish<<<g2, 64, 0, s>>>(scratch, C, outputs, splits, stride);
+    check_launch("skinny_finish");
+    return;
+  }
+  if (n == 1) {
+    if (k <= 32) {
+      dim3 grid((unsigned)((m + 255) / 256), (unsigned)batch);
+      gemv_rows_thread<<<grid, 256, 0, s>>>(A, B, C, m, (int)k, stride);
+    } else {
+      dim3 grid((unsigned)((m * 32 + 255) / 256), (unsigned)batch);
+      gemv_rows_warp<<<grid, 256, 0, s>>>(A, B, C, m, k, stride);
+    }
+    check_launch("gemv_rows");
+    return;
+  }
+  if (m == 1) {
+    if (n >= 256) {
+      dim3 grid((unsigned)((n + 255) / 256), (unsigned)batch);
+      gemv_cols_thread<<<grid, 256, 0, s>>>(A, B, C, n, k, stride);
+    } else {
+      dim3 grid((unsigned)n, (unsigned)batch);
+      gemv_cols_block<<<grid, 256, 0, s>>>(A, B, C, n, k, stride);
+    }
+    check_launch("gemv_cols");
+    return;
+  }
+  if (m > 0x7fffffffull || n > 0x7fffffffull || k > 0x7fffffffull)
+    throw std::string("ERROR (qflex_gb300: cgemm) --> dimension exceeds 2^31");
+  if (n <= 32)
+    run_cgemm<256, 16, 16, 8, 2>(A, B, C, m, n, k, stride, batch, s);
+  else if (m <= 32)
+    run_cgemm<16, 256, 16, 2, 8>(A, B, C, m, n, k, stride, batch, s);
+  else
+    run_cgemm<128, 64, 16, 8, 4>(A, B, C, m, n, k, stride, batch, s);
+}
+
+void launch_reduce_amplitudes(const float2* results, std::uint64_t stride, const std::uint32_t* ptr,
+                              const std::uint32_t* leaves, int n_amps, double2* amps, int batch,
+                              cudaStream_t s) {
+  if (n_amps == 0) return;
+  dim3 grid((unsigned)((n_amps + 127) / 128), (unsigned)batch);
+  reduce_amplitudes_kernel<<<grid, 128, 0, s>>>(results, stride, ptr, leaves, n_amps, amps);
+  check_launch("reduce_amplitudes");
+}
+
+}  // namespace qfx

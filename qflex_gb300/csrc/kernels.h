@@ -1,0 +1,93 @@
+// Device kernels of the contraction path and their launch helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace qfx {
+
+// ---- 3D -> 2D flatten -------------------------------------------------------
+// One column = one active qubit's time column. Its 2D tensor element e is
+// <final| G_K(v_K(e)) ... G_1(v_1(e)) |init>, where every two-qubit half
+// reads its virtual digit v_t(e) = (e >> shift) & (V - 1) of its bond.
+struct ColumnDesc {
+  std::uint64_t out_offset;  // element offset of the 2D tensor in the arena
+  std::uint32_t size_log2;   // log2 of the 2D tensor's element count
+  std::uint32_t step_begin, step_end;
+  std::int32_t o_shift;      // bit of the (o) index, -1 when not terminal
+};
+
+struct StepDesc {
+  std::uint32_t kind;     // 1: 2x2 matrix; 2: two-qubit half (in, v, out)
+  std::uint32_t V;        // virtual dimension of a two-qubit half
+  std::uint32_t shift;    // bit position of the virtual digit
+  std::uint32_t mat;      // offset of the gate data in the matrix pool
+};
+
+void launch_flatten(const ColumnDesc* cols, int n_cols, std::uint32_t max_size_log2,
+                    const StepDesc* steps, const float2* mats, const std::uint8_t* init_bits,
+                    const std::uint8_t* final_bits, float2* arena, std::uint64_t arena_stride,
+                    int batch, cudaStream_t s);
+
+// ---- index permutation over binary digits --------------------------------------
+// The tensor is viewed as nbits binary digits; input digit p moves to output
+// digit perm[p]. A tile covers up to 10 digits: the low input digits (read
+// coalesced) and the digits that become the low output digits (written
+// coalesced); the remaining digits index the tiles.
+struct PermPlan {
+  std::uint32_t tile_bits;
+  std::uint32_t n_outer;                 // number of digits outside the tile
+  std::uint64_t n_tiles;                 // 2^n_outer
+  std::uint8_t outer_in[40], outer_out[40];
+  // Lookup tables split by the low / high five bits of a tile index j:
+  // [0],[1] input offset of tile element j (input order); [2],[3] output
+  // offset of output-order element j; [4],[5] its tile slot.
+  std::uint32_t tab[6][32];
+};
+
+void make_perm_plan(int nbits, const std::uint8_t* perm, PermPlan* plan);
+
+// Index schedule of the permutation kernel, shared by the device kernel and
+// the host-side schedule check.
+__host__ __device__ inline std::uint32_t perm_swizzle(std::uint32_t j) { return j ^ ((j >> 5) & 31u); }
+__host__ __device__ inline void perm_tile_base(const PermPlan& P, std::uint64_t t, std::uint64_t* bi,
+                                               std::uint64_t* bo) {
+  std::uint64_t i = 0, o = 0;
+  for (std::uint32_t q = 0; q < P.n_outer; ++q) {
+    const std::uint64_t bit = (t >> q) & 1u;
+    i |= bit << P.outer_in[q];
+    o |= bit << P.outer_out[q];
+  }
+  *bi = i;
+  *bo = o;
+}
+
+// Runs the kernel's schedule on host buffers (tile by tile, load phase then
+// store phase, through a 1024-slot swizzled tile). Tests use it to check the
+// plan and the index math without a GPU.
+void permute_schedule_on_host(const PermPlan& plan, const float2* src, float2* dst,
+                              std::uint64_t size);
+void launch_permute(const PermPlan& plan, const float2* src, float2* dst, std::uint64_t batch_stride,
+                    int batch, cudaStream_t s);
+
+// ---- complex64 products on CUDA cores -------------------------------------------
+// C[m,n] = A[m,k] * B[k,n], row-major, all three advanced by batch_stride
+// elements per batch entry. Products with m * n <= 64 and k >= 8192 split k
+// over many blocks; their partial sums go to `scratch` (kSkinnyScratchElems
+// float2, or nullptr to keep the one-block-per-output kernels).
+constexpr std::size_t kSkinnyScratchElems = std::size_t(1) << 20;
+int skinny_splits(std::size_t m, std::size_t n, std::size_t k, int batch);
+void launch_cgemm_fp32(const float2* A, const float2* B, float2* C, std::size_t m, std::size_t n,
+                       std::size_t k, std::uint64_t batch_stride, int batch, cudaStream_t s,
+                       float2* scratch);
+
+// ---- FP64 amplitude sums -------------------------------------------------------
+// amps[b * n_amps + a] += sum of results[b * stride + leaf] over the leaves
+// of amplitude a (CSR: leaves[ptr[a] .. ptr[a+1])), in leaf order.
+void launch_reduce_amplitudes(const float2* results, std::uint64_t stride, const std::uint32_t* ptr,
+                              const std::uint32_t* leaves, int n_amps, double2* amps, int batch,
+                              cudaStream_t s);
+
+}  // namespace qfx

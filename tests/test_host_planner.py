@@ -1,0 +1,112 @@
+"""Host logic of the engine through the C ABI, without a GPU: a planning-only
+context (device -1) parses, validates and plans exactly as a GPU context
+does, so its output states, mutated input states, product sequence and
+error texts are compared with the reference's golden fixtures."""
+import numpy as np
+import pytest
+
+from oracle import qflex_oracle as qo
+from qflex_gb300 import Context, QflexGb300Error, rqc
+
+
+@pytest.fixture(scope="module")
+def plan_ctx(built_lib):
+    return Context(-1)
+
+
+CASES = ["simple", "c1_4x5_d16", "rect4x4_cut_terminal", "c2_6x6_d24_partial_cut",
+         "fsim_3x4_off", "c3_7x7_d32_one_slice"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_plan_matches_reference(plan_ctx, ref_cases, name):
+    case = ref_cases[name]
+    limit = qo.parse_memory(case["memory_limit"])
+    for run in case["runs"]:
+        out = plan_ctx.evaluate(case["circuit"], case["ordering"], case["grid"], case["initial"],
+                                run["final"], limit)
+        assert [s for s, _ in out] == run["states"]
+        assert plan_ctx.initial_state() == run["initial_out"]
+        assert plan_ctx.final_state() == run["final_out"]
+        if run["gemms"]:
+            assert plan_ctx.gemms() == [tuple(g) for g in run["gemms"]]
+
+
+@pytest.mark.parametrize("name,fragment", [
+    ("err_memory_limit", "Required space (1.12 GB) exceeds memory limit (1 GB). Cancelling simulation."),
+    ("err_cut_after_expand", "Index: '(0,1),(0,2)' has to be equal to indices[0]: '(0,0),(0,1)'."),
+    ("err_bad_gate", "Invalid gate name provided: foo"),
+    ("err_bad_op", "Parsing failed on line: '' with error: Received an invalid operation in config."),
+])
+def test_errors_match_reference(plan_ctx, ref_cases, name, fragment):
+    case = ref_cases[name]
+    assert fragment in case["runs"][0]["error"]
+    with pytest.raises(QflexGb300Error) as e:
+        plan_ctx.evaluate(case["circuit"], case["ordering"], case["grid"], case["initial"],
+                          case["runs"][0]["final"], qo.parse_memory(case["memory_limit"]))
+    assert fragment in str(e.value)
+    assert e.value.code == 1
+
+
+def test_reference_plan_bytes_equal_oracle(plan_ctx, ref_cases):
+    case = ref_cases["c3_7x7_d32_one_slice"]
+    plan_ctx.evaluate(case["circuit"], case["ordering"], case["grid"], "", "", 1 << 40)
+    inp = qo.Input(qo.Circuit.loads(case["circuit"]), qo.load_ordering(case["ordering"]),
+                   qo.Grid.loads(case["grid"]))
+    ops = qo.parse_ordering(inp.ordering, inp.grid)
+    base, fq, _ = qo.output_states(inp.grid, ops, "0" * 49, "")
+    g2 = qo.build_grid(inp.circuit, inp.grid, "0" * 49, base, fq, ops, np.complex64)
+    assert plan_ctx.stats()["reference_bytes"] == qo.planned_bytes(ops, g2)
+
+
+def test_validation_errors(plan_ctx):
+    c = rqc.random_circuit(2, 2, 4, 0)
+    g = rqc.grid_text(2, 2)
+    cases = [
+        ("expand a 0\nexpand a 0\nexpand a 1\nexpand a 2\nexpand a 3\n", "is contracted multiple times"),
+        ("expand a 0\ncut () 0 1\nexpand a 1\n", "is added to non-empty patch a after a cut"),
+        ("cut (0,1 0 1\n", "Cut values must be comma-separated ints"),
+        ("expand a 7\n", "Index 7 must be within grid boundaries."),
+        ("cut () 0 1\ncut () 1 0\nexpand a 0\n", "is cut multiple times"),
+    ]
+    for ordering, fragment in cases:
+        with pytest.raises(QflexGb300Error) as e:
+            plan_ctx.evaluate(c, ordering, g, "", "", 1 << 30)
+        assert fragment in str(e.value), (ordering, str(e.value))
+
+
+def test_circuit_format_errors(plan_ctx):
+    g = rqc.grid_text(1, 2)
+    o = "expand a 0\nexpand a 1\n"
+    for circuit, fragment in [
+        ("2\n0 h 0\n0 h 0\n", "Qubits can only used once per cycle."),
+        ("2\n1 h 0\n0 h 1\n", "Cycle number can only increase."),
+        ("2\n0 h(0 0\n", "Not-matching parentheses."),
+        ("2\n0 h\n", "Gate must be specified as"),
+        ("2\n0 foo 0\n", "Invalid gate name provided: foo"),
+        ("3\n0 h 0\n", "does not match the number of active qubits"),
+        ("2\n0 cz 0 2\n", "must correspond to an active qubit"),
+    ]:
+        with pytest.raises(QflexGb300Error) as e:
+            plan_ctx.evaluate(circuit, o, g, "", "", 1 << 30)
+        assert fragment in str(e.value), (circuit, str(e.value))
+
+
+def test_state_length_errors(plan_ctx):
+    c = rqc.random_circuit(1, 2, 2, 0)
+    with pytest.raises(QflexGb300Error) as e:
+        plan_ctx.evaluate(c, "expand a 0\nexpand a 1\n", "1 1\n", "000", "", 1 << 30)
+    assert "Size of initial_conf: 3, must be equal to the number of qubits: 2." in str(e.value)
+    with pytest.raises(QflexGb300Error) as e:
+        plan_ctx.evaluate(c, "expand a 0\nexpand a 1\n", "1 1\n", "00", "0", 1 << 30)
+    assert "Size of final_conf: 1, must be equal to size of initial_conf: 2." in str(e.value)
+
+
+def test_workload_plans(plan_ctx):
+    """The benchmark workloads plan within the documented memory and work."""
+    for name, max_gb in (("c1", 0.01), ("c2", 1.0), ("c3", 1.5)):
+        c, o, g, ini, fins = rqc.workload(name)
+        plan_ctx.evaluate(c, o, g, ini, fins[0], 1 << 40)
+        s = plan_ctx.stats()
+        assert s["arena_bytes"] < max_gb * 2 ** 30
+        assert s["gemm_flop"] > 0
