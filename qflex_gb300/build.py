@@ -19,6 +19,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libqflex_gb300.so"
+CLI = PKG / "qflex"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -62,8 +63,15 @@ def build(verbose: bool = False) -> Path:
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    cli_src = PKG / "cli" / "qflex_cli.cpp"
+    if not CLI.exists() or CLI.stat().st_mtime < max(LIB.stat().st_mtime, cli_src.stat().st_mtime):
+        cmd = ["g++", "-O2", "-std=c++17", "-I", str(PKG.parent / "include"), str(cli_src),
+               "-L", str(PKG), "-lqflex_gb300", "-Wl,-rpath,$ORIGIN", "-o", str(CLI)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"CLI build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     if verbose:
-        print(f"built {LIB}")
+        print(f"built {LIB} and {CLI}")
     return LIB
 
 

@@ -282,8 +282,8 @@ int qflex_gb300_multiply(qflex_gb300_context* ctx, const void* A, const void* B,
     if (batch == 0 || m == 0 || n == 0) return;
     if (batch > 65535) throw QFX_ERR("batch must be at most 65535.");
     cudaSetDevice(ctx->engine->device());
-    qfx::launch_cgemm_fp32((const float2*)A, (const float2*)B, (float2*)C, m, n, k, batch_stride,
-                           (int)batch, ctx->engine->stream(), ctx->engine->skinny_scratch());
+    ctx->engine->multiply((const float2*)A, (const float2*)B, (float2*)C, m, n, k, batch_stride,
+                          (int)batch);
   });
 }
 

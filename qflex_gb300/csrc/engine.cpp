@@ -3,6 +3,8 @@
 // one batched replay per group of final states.
 #include "engine.h"
 
+#include "tc_gemm.h"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -30,6 +32,8 @@ struct Engine::Plan {
   Network net;
   Program prog;
   std::vector<PermPlan> perm;  // indexed like prog.ops (unused for GEMM ops)
+  int precision = -1;          // precision the program was planned for
+  std::size_t tc_ws_elems = 0; // split-plane workspace of one batch entry
   std::uint32_t max_size_log2 = 0;
   ColumnDesc* d_cols = nullptr;
   StepDesc* d_steps = nullptr;
@@ -73,8 +77,52 @@ Engine::~Engine() {
 }
 
 void Engine::set_precision(int p) {
-  if (p != FP32) throw QFX_ERR("Precision mode ", p, " is not available in this build.");
+  if (p != FP32 && p != TF32X3) throw QFX_ERR("Precision mode ", p, " is not available in this build.");
   precision_ = p;
+}
+
+int* Engine::error_flag() { return (int*)reserve(sizeof(int) * 4, 5); }
+
+float* Engine::tc_workspace(std::size_t elems) {
+  return (float*)reserve(std::max<std::size_t>(elems, 1) * sizeof(float), 4);
+}
+
+void Engine::check_error_flag() {
+  int h = 0;
+  QFX_CUDA(cudaMemcpyAsync(&h, error_flag(), sizeof(int), cudaMemcpyDeviceToHost, stream_));
+  QFX_CUDA(cudaStreamSynchronize(stream_));
+  if (h != 0) {
+    QFX_CUDA(cudaMemsetAsync(error_flag(), 0, sizeof(int), stream_));
+    throw QFX_ERR("A tensor-core pipeline wait expired (code ", h, "); results discarded.");
+  }
+}
+
+void Engine::multiply(const float2* A, const float2* B, float2* C, std::size_t m, std::size_t n,
+                      std::size_t k, std::uint64_t stride, int batch) {
+  if (precision_ == TF32X3 && tc_eligible(m, n, k)) {
+    // The tensor-core kernel reads B as [n][k]: transpose into the front of
+    // the workspace, split planes after it.
+    const std::size_t bt = ((n * k * (std::size_t)batch + 63) / 64) * 64;
+    float* ws = tc_workspace(2 * bt + tc_workspace_elems(m, n, k) * (std::size_t)batch);
+    float2* Bt = reinterpret_cast<float2*>(ws);
+    int nbits = 0;
+    std::uint8_t perm[40] = {};
+    int ln = 0, lk = 0;
+    while ((std::size_t(1) << ln) < n) ++ln;
+    while ((std::size_t(1) << lk) < k) ++lk;
+    if ((std::size_t(1) << ln) == n && (std::size_t(1) << lk) == k) {
+      nbits = ln + lk;
+      for (int b = 0; b < ln; ++b) perm[b] = (std::uint8_t)(lk + b);   // n digits move up
+      for (int b = 0; b < lk; ++b) perm[ln + b] = (std::uint8_t)b;     // k digits move down
+      PermPlan plan;
+      make_perm_plan(nbits, perm, &plan);
+      for (int b = 0; b < batch; ++b)
+        launch_permute(plan, B + (std::size_t)b * stride, Bt + (std::size_t)b * n * k, 0, 1, stream_);
+      launch_cgemm_tf32x3(A, Bt, C, m, n, k, stride, n * k, batch, ws + 2 * bt, error_flag(), stream_);
+      return;
+    }
+  }
+  launch_cgemm_fp32(A, B, C, m, n, k, stride, batch, stream_, skinny_scratch());
 }
 
 void Engine::set_stream(cudaStream_t s) {
@@ -116,6 +164,8 @@ Engine::Plan* Engine::get_plan(const std::string& circuit, const std::string& or
   key += ordering;
   key += '\x01';
   key += grid;
+  key += '\x01';
+  key += std::to_string(precision_);
   if (plan_ && plan_->key == key) return plan_.get();
   auto p = std::make_unique<Plan>();
   p->key = std::move(key);
@@ -189,14 +239,18 @@ T* upload(const std::vector<T>& v) {
 
 }  // namespace
 
-void Engine::run_program(Plan& p, int batch, float2* arena) {
+void Engine::run_program(Plan& p, int batch, float2* arena, float* tc_ws) {
   const Program& prog = p.prog;
   const std::uint64_t stride = prog.arena_elems;
   float2* scratch = skinny_scratch();
+  int* err = error_flag();
   for (std::size_t i = 0; i < prog.ops.size(); ++i) {
     const DevOp& op = prog.ops[i];
     if (op.kind == DevOp::PERMUTE) {
       launch_permute(p.perm[i], arena + op.a, arena + op.c, stride, batch, stream_);
+    } else if (op.b_nk) {
+      launch_cgemm_tf32x3(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, stride,
+                          batch, tc_ws, err, stream_);
     } else {
       launch_cgemm_fp32(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, batch,
                         stream_, scratch);
@@ -236,11 +290,18 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
   }
   if (!p.built) {
     p.net = build_network(p.circuit, p.grid, initial, results[0].final_state, final_qubits, p.ops);
+    std::function<bool(std::size_t, std::size_t, std::size_t)> b_kmajor;
+    if (precision_ == TF32X3) b_kmajor = tc_eligible;
     try {
-      p.prog = plan_contraction(p.net, p.ops, results[0].states.size(), INFINITY);
+      p.prog = plan_contraction(p.net, p.ops, results[0].states.size(), INFINITY, b_kmajor);
     } catch (const std::string& e) {
       throw QFX_WRAP("ContractGrid", e);
     }
+    p.precision = precision_;
+    p.tc_ws_elems = 0;
+    for (const auto& op : p.prog.ops)
+      if (op.kind == DevOp::GEMM && op.b_nk)
+        p.tc_ws_elems = std::max(p.tc_ws_elems, tc_workspace_elems(op.m, op.n, op.k));
     p.perm.resize(p.prog.ops.size());
     for (std::size_t i = 0; i < p.prog.ops.size(); ++i)
       if (p.prog.ops[i].kind == DevOp::PERMUTE)
@@ -303,12 +364,18 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
   // How many final states fit on the device at once.
   std::size_t free_b = 0, total_b = 0;
   QFX_CUDA(cudaMemGetInfo(&free_b, &total_b));
-  const std::size_t have = bufs_.size() > 0 ? bufs_[0].bytes : 0;
+  std::size_t have = 0;
+  for (int slot : {0, 4})
+    if ((int)bufs_.size() > slot) have += bufs_[slot].bytes;
   const std::size_t usable = free_b + have > (std::size_t(2) << 30) ? free_b + have - (std::size_t(2) << 30) : 0;
-  int chunk = (int)std::max<std::size_t>(1, std::min<std::size_t>((std::size_t)total, usable / std::max<std::size_t>(arena_bytes, 1)));
+  const std::size_t per_entry = arena_bytes + p.tc_ws_elems * sizeof(float);
+  int chunk = (int)std::max<std::size_t>(1, std::min<std::size_t>((std::size_t)total, usable / std::max<std::size_t>(per_entry, 1)));
   chunk = std::min(chunk, 65535);
 
   float2* arena = (float2*)reserve(arena_bytes * (std::size_t)chunk, 0);
+  float* tc_ws = p.tc_ws_elems ? tc_workspace(p.tc_ws_elems * (std::size_t)chunk) : nullptr;
+  skinny_scratch();
+  QFX_CUDA(cudaMemsetAsync(error_flag(), 0, sizeof(int), stream_));
   double2* d_amps = (double2*)reserve(std::max<std::size_t>(n_amps, 1) * sizeof(double2) * (std::size_t)chunk, 1);
   std::uint8_t* d_bits = (std::uint8_t*)reserve(std::max<std::size_t>(n_cols, 1) * 2 * (std::size_t)chunk, 2);
 
@@ -334,7 +401,7 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
     QFX_CUDA(cudaEventRecord(ev0_, stream_));
     launch_flatten(p.d_cols, (int)n_cols, p.max_size_log2, p.d_steps, p.d_mats, d_bits,
                    d_bits + n_cols * (std::size_t)nb, arena, prog.arena_elems, nb, stream_);
-    run_program(p, nb, arena);
+    run_program(p, nb, arena, tc_ws);
     launch_reduce_amplitudes(arena + prog.results_offset, prog.arena_elems, p.d_ptr, p.d_leaves,
                              (int)n_amps, d_amps, nb, stream_);
     QFX_CUDA(cudaEventRecord(ev1_, stream_));
@@ -353,6 +420,7 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
       }
     }
   }
+  if (p.tc_ws_elems) check_error_flag();
   stats_.device_ms = ms_total;
   stats_.batch = (std::size_t)chunk;
   return results;

@@ -64,11 +64,21 @@ class Engine {
   void* reserve(std::size_t bytes, int slot);
   // Partial-sum buffer of the split-k skinny products (kSkinnyScratchElems).
   float2* skinny_scratch();
+  // Device int set by tensor-core kernels whose pipeline waits expired.
+  int* error_flag();
+  // Throws (and clears the flag) when a kernel reported an expired wait.
+  void check_error_flag();
+  // Split planes of the tensor-core products.
+  float* tc_workspace(std::size_t elems);
+  // C[m,n] = A[m,k] * B[k,n] (row-major complex64) in the context's
+  // precision; `batch` products at `stride` elements.
+  void multiply(const float2* A, const float2* B, float2* C, std::size_t m, std::size_t n,
+                std::size_t k, std::uint64_t stride, int batch);
 
  private:
   struct Plan;
   Plan* get_plan(const std::string& circuit, const std::string& ordering, const std::string& grid);
-  void run_program(Plan& p, int batch, float2* arena);
+  void run_program(Plan& p, int batch, float2* arena, float* tc_ws);
 
   int device_;
   int precision_;

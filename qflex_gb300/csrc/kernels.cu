@@ -309,17 +309,25 @@ __global__ void __launch_bounds__(256) skinny_partial(const float2* __restrict__
   }
 }
 
+// One warp per output: lane l adds partials l, l + 32, ... in FP64, then a
+// fixed shuffle tree combines the lanes.
 __global__ void skinny_finish(const float2* __restrict__ partial, float2* __restrict__ C, int outputs,
                               int splits, std::uint64_t batch_stride) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
   if (r >= outputs) return;
   const float2* p = partial + (std::uint64_t(blockIdx.y) * outputs + r) * splits;
   double re = 0, im = 0;
-  for (int s = 0; s < splits; ++s) {
+  for (int s = lane; s < splits; s += 32) {
     re += double(p[s].x);
     im += double(p[s].y);
   }
-  C[std::uint64_t(blockIdx.y) * batch_stride + r] = make_float2(float(re), float(im));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    re += __shfl_xor_sync(0xffffffffu, re, o);
+    im += __shfl_xor_sync(0xffffffffu, im, o);
+  }
+  if (lane == 0) C[std::uint64_t(blockIdx.y) * batch_stride + r] = make_float2(float(re), float(im));
 }
 
 __global__ void reduce_amplitudes_kernel(const float2* __restrict__ results, std::uint64_t stride,
@@ -474,8 +482,8 @@ void launch_cgemm_fp32(const float2* A, const float2* B, float2* C, std::size_t 
     dim3 g1((unsigned)(outputs * splits), (unsigned)batch);
     skinny_partial<<<g1, 256, 0, s>>>(A, B, scratch, (int)n, k, splits, stride);
     check_launch("skinny_partial");
-    dim3 g2((unsigned)((outputs + 63) / 64), (unsigned)batch);
-    skinny_finish<<<g2, 64, 0, s>>>(scratch, C, outputs, splits, stride);
+    dim3 g2((unsigned)((outputs * 32 + 127) / 128), (unsigned)batch);
+    skinny_finish<<<g2, 128, 0, s>>>(scratch, C, outputs, splits, stride);
     check_launch("skinny_finish");
     return;
   }

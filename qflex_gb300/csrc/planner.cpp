@@ -50,9 +50,15 @@ std::vector<std::string> concat(std::vector<std::string> a, const std::vector<st
   return a;
 }
 
+// A tensor during planning. `idx`/`dim` mirror the reference's index order
+// (its in-place reorders decide its error messages); `phys`/`pdim` are the
+// order the data actually has in its buffer, which the planner changes only
+// when a product or a projection needs another layout.
 struct STensor {
   std::vector<std::string> idx;
   std::vector<std::size_t> dim;
+  std::vector<std::string> phys;
+  std::vector<std::size_t> pdim;
   int buf = -1;
   std::size_t off = 0;
   std::size_t size() const {
@@ -128,8 +134,9 @@ double reference_plan_bytes(const Network& net, const std::vector<Op>& ops) {
 
 class Planner {
  public:
-  Planner(const Network& net, const std::vector<Op>& ops, std::size_t n_amps)
-      : net_(net), ops_(ops) {
+  Planner(const Network& net, const std::vector<Op>& ops, std::size_t n_amps,
+          std::function<bool(std::size_t, std::size_t, std::size_t)> b_kmajor)
+      : net_(net), ops_(ops), b_kmajor_(std::move(b_kmajor)) {
     prog_.n_amplitudes = n_amps;
   }
 
@@ -138,7 +145,7 @@ class Planner {
     prog_.column_offset.resize(net_.columns.size());
     for (std::size_t c = 0; c < net_.columns.size(); ++c) {
       const auto& col = net_.columns[c];
-      STensor t{col.indices, col.dims, -1, 0};
+      STensor t{col.indices, col.dims, col.indices, col.dims, -1, 0};
       t.buf = alloc(t.size());
       prog_.column_offset[c] = bufs_[t.buf].off;
       grid_[col.pos] = t;
@@ -186,20 +193,31 @@ class Planner {
   }
   std::size_t addr(const STensor& t) const { return bufs_[t.buf].off + t.off; }
 
-  // Tensor::reorder (src/tensor.cpp:866-911) as an out-of-place permute.
-  void reorder(STensor& t, const std::vector<std::string>& order) {
-    if (order.empty() && t.idx.empty()) return;
+  // Tensor::reorder (src/tensor.cpp:866-911): the reference's index order
+  // changes; the data is moved only when physical() asks for it.
+  static void reorder(STensor& t, const std::vector<std::string>& order) {
     if (order == t.idx) return;
-    const std::size_t r = t.idx.size();
+    std::vector<std::size_t> nd(order.size());
+    for (std::size_t p = 0; p < order.size(); ++p) nd[p] = t.dim_of(order[p]);
+    t.idx = order;
+    t.dim = nd;
+  }
+
+  // Moves the data of `t` into index order `order` (an out-of-place
+  // permute into a fresh buffer) unless it is already laid out that way.
+  void physical(STensor& t, const std::vector<std::string>& order) {
+    if (order.empty() && t.phys.empty()) return;
+    if (order == t.phys) return;
+    const std::size_t r = t.phys.size();
     std::vector<int> lg(r);
-    for (std::size_t i = 0; i < r; ++i) lg[i] = ilog2_exact(t.dim[i]);
+    for (std::size_t i = 0; i < r; ++i) lg[i] = ilog2_exact(t.pdim[i]);
     std::vector<int> s_old(r, 0);
     for (std::size_t i = r; i-- > 1;) s_old[i - 1] = s_old[i] + lg[i];
     std::vector<std::size_t> new_pos(r);
     std::vector<std::size_t> new_dim(r);
     for (std::size_t i = 0; i < r; ++i) {
-      new_pos[i] = std::find(order.begin(), order.end(), t.idx[i]) - order.begin();
-      new_dim[new_pos[i]] = t.dim[i];
+      new_pos[i] = std::find(order.begin(), order.end(), t.phys[i]) - order.begin();
+      new_dim[new_pos[i]] = t.pdim[i];
     }
     std::vector<int> s_new(r, 0);
     for (std::size_t p = r; p-- > 1;) s_new[p - 1] = s_new[p] + ilog2_exact(new_dim[p]);
@@ -222,8 +240,8 @@ class Planner {
       t.buf = nb;
       t.off = 0;
     }
-    t.idx = order;
-    t.dim = new_dim;
+    t.phys = order;
+    t.pdim = new_dim;
   }
 
   // multiply (src/tensor.cpp:1045-1194): C(left, right) = A(left, common) *
@@ -244,10 +262,17 @@ class Planner {
     }
     reorder(A, concat(left, common));
     reorder(B, concat(common, right));
+    // Tensor-core products read B as (right, common) rows (K-major); the
+    // CUDA-core kernels read the reference's (common, right) layout.
+    const bool b_nk = b_kmajor_(m, n, k);
+    physical(A, concat(left, common));
+    physical(B, b_nk ? concat(right, common) : concat(common, right));
     STensor C;
     C.idx = concat(left, right);
     for (const auto& x : left) C.dim.push_back(A.dim_of(x));
     for (const auto& x : right) C.dim.push_back(B.dim_of(x));
+    C.phys = C.idx;
+    C.pdim = C.dim;
     C.buf = alloc(m * n);
     DevOp op{DevOp::GEMM};
     op.a = addr(A);
@@ -256,6 +281,7 @@ class Planner {
     op.m = m;
     op.n = n;
     op.k = k;
+    op.b_nk = b_nk;
     const auto key = std::make_tuple(m, n, k);
     auto it = shape_index_.find(key);
     if (it == shape_index_.end()) {
@@ -299,6 +325,7 @@ class Planner {
         STensor& ta = grid_.at(op.tensors[0]);
         STensor copy_a;
         assign(copy_a, ta);
+        lead_with(copy_a, index);
         std::vector<std::size_t> values = op.values;
         if (values.empty()) {
           if (std::find(copy_a.idx.begin(), copy_a.idx.end(), index) == copy_a.idx.end())
@@ -310,6 +337,7 @@ class Planner {
           STensor& tb = grid_.at(op.tensors[1]);
           STensor copy_b;
           assign(copy_b, tb);
+          lead_with(copy_b, index);
           for (std::size_t v : values) {
             project(copy_a, index, v, grid_.at(op.tensors[0]));
             project(copy_b, index, v, grid_.at(op.tensors[1]));
@@ -368,12 +396,26 @@ class Planner {
     if (value >= src.dim[0])
       throw QFX_ERR("Failed to call project(). Error:\n\t[index_value: ", value,
                     " must be contained in [0, ", src.dim[0], ").]");
+    if (src.phys.empty() || src.phys[0] != index)
+      throw QFX_ERR("Projected index ", index, " is not leading in memory.");
     STensor view;
     view.idx.assign(src.idx.begin() + 1, src.idx.end());
     view.dim.assign(src.dim.begin() + 1, src.dim.end());
+    view.phys.assign(src.phys.begin() + 1, src.phys.end());
+    view.pdim.assign(src.pdim.begin() + 1, src.pdim.end());
     view.buf = src.buf;
     view.off = src.off + value * (src.size() / src.dim[0]);
     assign(dst, view);
+  }
+
+  // Makes the cut index leading in memory when it leads the reference's
+  // order but not the buffer (after a tensor-core layout of the tensor).
+  void lead_with(STensor& t, const std::string& index) {
+    if (t.idx.empty() || t.idx[0] != index || t.phys[0] == index) return;
+    std::vector<std::string> order{index};
+    for (const auto& x : t.phys)
+      if (x != index) order.push_back(x);
+    physical(t, order);
   }
 
   struct Buf {
@@ -383,6 +425,7 @@ class Planner {
   };
   const Network& net_;
   const std::vector<Op>& ops_;
+  std::function<bool(std::size_t, std::size_t, std::size_t)> b_kmajor_;
   Program prog_;
   std::vector<Buf> bufs_;
   std::vector<int> free_[64];
@@ -397,13 +440,15 @@ class Planner {
 }  // namespace
 
 Program plan_contraction(const Network& net, const std::vector<Op>& ops, std::size_t n_amplitudes,
-                         double memory_limit) {
+                         double memory_limit,
+                         std::function<bool(std::size_t, std::size_t, std::size_t)> b_kmajor) {
   const double ref_bytes = reference_plan_bytes(net, ops);
   if (ref_bytes > memory_limit)
     throw QFX_ERR("Failed to call Initialize(). Error:\n\t[Required space (",
                   readable_memory_string(ref_bytes), ") exceeds memory limit (",
                   readable_memory_string(memory_limit), "). Cancelling simulation.]");
-  Planner p(net, ops, n_amplitudes);
+  if (!b_kmajor) b_kmajor = [](std::size_t, std::size_t, std::size_t) { return false; };
+  Planner p(net, ops, n_amplitudes, std::move(b_kmajor));
   Program prog = p.run();
   prog.reference_bytes = ref_bytes;
   return prog;

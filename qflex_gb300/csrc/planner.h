@@ -9,6 +9,7 @@
 #pragma once
 
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -25,6 +26,7 @@ struct DevOp {
   int nbits = 0;                    // PERMUTE: log2(size)
   std::uint8_t perm[40] = {};       // PERMUTE: output bit of each input bit
   int shape_id = -1;                // GEMM: index into Program::shapes
+  bool b_nk = false;                // GEMM: B stored as [n][k] (K-major)
 };
 
 struct GemmShape {
@@ -53,7 +55,11 @@ struct Program {
 // reference's errors (std::string) for orderings the reference rejects at
 // contraction time, and the memory-limit error before anything is
 // allocated.
+// `b_kmajor(m, n, k)` tells whether the product of that shape runs on a
+// kernel that reads B as [n][k] rows (the tensor-core path); by default
+// every product reads the reference's [k][n] layout.
 Program plan_contraction(const Network& net, const std::vector<Op>& ops,
-                         std::size_t n_amplitudes, double memory_limit);
+                         std::size_t n_amplitudes, double memory_limit,
+                         std::function<bool(std::size_t, std::size_t, std::size_t)> b_kmajor = {});
 
 }  // namespace qfx

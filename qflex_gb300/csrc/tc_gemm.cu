@@ -1,0 +1,362 @@
+// Complex64 products on the sm_103a tensor cores (tcgen05 + TMEM + TMA),
+// split precision.
+//
+// C = A * B with A (m x k) and B given as Bt (n x k), both K-major complex64.
+// Each complex operand is split into four real planes -- re_hi, re_lo,
+// im_hi, im_lo -- with x = hi + lo, hi and lo exactly representable in
+// TF32 (round-to-nearest), so x is carried to ~22 significant bits. The
+// product keeps the three leading terms of every real product
+// (hi*hi + hi*lo + lo*hi) and the complex product uses four real products:
+//   C_re = Ar Br - Ai Bi,   C_im = Ar Bi + Ai Br,
+// i.e. 12 TF32 MMAs per k-step, accumulated in FP32 in TMEM (C_re in
+// columns [0, BN), C_im in [BN, 2 BN)). The minus sign is the instruction
+// descriptor's negate-A bit.
+//
+// Kernel structure (one 128 x 128 output tile per CTA, 192 threads):
+//   warp 0      TMA producer: one 4-D box per operand and stage brings all
+//               four planes (k-step of 8 fp32 = one 32-byte swizzle row)
+//   warp 1      TMEM allocation and the single MMA-issuing thread
+//   warps 2..5  epilogue: tcgen05.ld of the 128 TMEM lanes -> complex64
+// Every mbarrier wait is bounded in time; on expiry the CTA records an
+// error code, stops issuing work, waits (bounded) for what it issued and
+// frees its TMEM before returning.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "kernels.h"
+#include "tc_gemm.h"
+
+namespace qfx {
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 8;
+constexpr int STAGES = 6;
+constexpr int PLANE_A = BM * BK * 4;                 // bytes of one plane tile
+constexpr int PLANE_B = BN * BK * 4;
+constexpr int STAGE_BYTES = 4 * PLANE_A + 4 * PLANE_B;
+constexpr int TMEM_COLS = 2 * BN;
+constexpr int THREADS = 192;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s per wait
+
+__device__ __forceinline__ std::uint32_t smem_u32(const void* p) {
+  return static_cast<std::uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ unsigned long long now_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(std::uint64_t* bar, std::uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(std::uint64_t* bar, std::uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_test(std::uint64_t* bar, std::uint32_t parity) {
+  std::uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: false (and an error code) when the phase does not complete
+// within WAIT_NS or another warp of the CTA has already given up.
+__device__ __forceinline__ bool mbar_wait(std::uint64_t* bar, std::uint32_t parity, volatile int* abort_flag,
+                                          int* err, int code) {
+  const unsigned long long t0 = now_ns();
+  while (!mbar_test(bar, parity)) {
+    if (*abort_flag) return false;
+    if (now_ns() - t0 > WAIT_NS) {
+      *abort_flag = 1;
+      atomicExch(err, code);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_4d(const CUtensorMap* map, std::uint64_t* bar, void* dst, int c0,
+                                            int c1, int c2, int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+      "%5}], [%6];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<std::uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, rows of 32 bytes in the
+// 32-byte swizzle, 8-row groups 256 bytes apart.
+__device__ __forceinline__ std::uint64_t smem_desc_sw32(std::uint32_t addr) {
+  std::uint64_t d = 0;
+  d |= std::uint64_t((addr & 0x3FFFF) >> 4);       // start address
+  d |= std::uint64_t(1) << 16;                     // leading byte offset (unused here)
+  d |= std::uint64_t(256 >> 4) << 32;              // stride byte offset
+  d |= std::uint64_t(1) << 46;                     // descriptor version
+  d |= std::uint64_t(6) << 61;                     // 32-byte swizzle
+  return d;
+}
+
+// Instruction descriptor, kind::tf32: D = F32, A = B = TF32, both K-major.
+__host__ __device__ constexpr std::uint32_t idesc_tf32(int m, int n, bool negate_a) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | (negate_a ? (1u << 13) : 0u) |
+         (std::uint32_t(n >> 3) << 17) | (std::uint32_t(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_tf32(std::uint32_t d_tmem, std::uint64_t a, std::uint64_t b,
+                                          std::uint32_t idesc, std::uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void umma_commit(std::uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
+#define TMEM_LD32(taddr, r)                                                                            \
+  asm volatile(                                                                                        \
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15," \
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"                       \
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),          \
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),       \
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),    \
+        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),    \
+        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])                                            \
+      : "r"(taddr))
+
+__global__ void __launch_bounds__(THREADS, 1)
+    cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                        float2* __restrict__ C, int m, int n, int k, std::uint64_t c_batch_stride,
+                        int* __restrict__ err) {
+  extern __shared__ __align__(1024) std::uint8_t smem_raw[];
+  std::uint8_t* smem = reinterpret_cast<std::uint8_t*>((reinterpret_cast<std::uintptr_t>(smem_raw) + 1023) &
+                                                       ~std::uintptr_t(1023));
+  std::uint64_t* full = reinterpret_cast<std::uint64_t*>(smem + STAGES * STAGE_BYTES);
+  std::uint64_t* empty = full + STAGES;
+  std::uint64_t* tmem_full = empty + STAGES;
+  std::uint32_t* tmem_slot = reinterpret_cast<std::uint32_t*>(tmem_full + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int tiles_m = (m + BM - 1) / BM;
+  const int m0 = (blockIdx.x % tiles_m) * BM;
+  const int n0 = (blockIdx.x / tiles_m) * BN;
+  const int batch = blockIdx.z;
+  const int kblocks = (k + BK - 1) / BK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(tmem_full, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const std::uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // Producer.
+    int issued = 0;
+    for (int kb = 0; kb < kblocks; ++kb) {
+      const int s = kb % STAGES;
+      if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) - 1) & 1, abort_flag, err, 1)) break;
+      std::uint8_t* st = smem + s * STAGE_BYTES;
+      mbar_expect_tx(&full[s], STAGE_BYTES);
+      tma_load_4d(&map_a, &full[s], st, kb * BK, m0, 0, batch);
+      tma_load_4d(&map_b, &full[s], st + 4 * PLANE_A, kb * BK, n0, 0, batch);
+      issued = kb + 1;
+    }
+    if (*abort_flag) {
+      // Let the copies already issued land before the CTA's shared memory
+      // is released (bounded as well).
+      for (int kb = issued > STAGES ? issued - STAGES : 0; kb < issued; ++kb) {
+        const unsigned long long t0 = now_ns();
+        while (!mbar_test(&full[kb % STAGES], (kb / STAGES) & 1) && now_ns() - t0 < WAIT_NS) {
+        }
+      }
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer. Planes in a stage: A re_hi, re_lo, im_hi, im_lo, then B.
+    const std::uint32_t idp = idesc_tf32(BM, BN, false), idn = idesc_tf32(BM, BN, true);
+    const std::uint32_t d_re = tmem, d_im = tmem + BN;
+    for (int kb = 0; kb < kblocks; ++kb) {
+      const int s = kb % STAGES;
+      if (!mbar_wait(&full[s], (kb / STAGES) & 1, abort_flag, err, 2)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const std::uint32_t a0 = smem_u32(smem + s * STAGE_BYTES);
+      const std::uint32_t b0 = a0 + 4 * PLANE_A;
+      const std::uint64_t arh = smem_desc_sw32(a0), arl = smem_desc_sw32(a0 + PLANE_A),
+                          aih = smem_desc_sw32(a0 + 2 * PLANE_A), ail = smem_desc_sw32(a0 + 3 * PLANE_A);
+      const std::uint64_t brh = smem_desc_sw32(b0), brl = smem_desc_sw32(b0 + PLANE_B),
+                          bih = smem_desc_sw32(b0 + 2 * PLANE_B), bil = smem_desc_sw32(b0 + 3 * PLANE_B);
+      const std::uint32_t acc = kb > 0 ? 1u : 0u;
+      umma_tf32(d_re, arh, brh, idp, acc);
+      umma_tf32(d_re, arh, brl, idp, 1);
+      umma_tf32(d_re, arl, brh, idp, 1);
+      umma_tf32(d_re, aih, bih, idn, 1);
+      umma_tf32(d_re, aih, bil, idn, 1);
+      umma_tf32(d_re, ail, bih, idn, 1);
+      umma_tf32(d_im, arh, bih, idp, acc);
+      umma_tf32(d_im, arh, bil, idp, 1);
+      umma_tf32(d_im, arl, bih, idp, 1);
+      umma_tf32(d_im, aih, brh, idp, 1);
+      umma_tf32(d_im, aih, brl, idp, 1);
+      umma_tf32(d_im, ail, brh, idp, 1);
+      umma_commit(&empty[s]);
+    }
+    umma_commit(tmem_full);
+  } else if (warp >= 2) {
+    // Epilogue: warp w reads TMEM lanes [32 (w % 4), 32 (w % 4) + 32).
+    const int q = warp % 4;
+    const int row = q * 32 + lane;
+    const bool ok = mbar_wait(tmem_full, 0, abort_flag, err, 3);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (ok) {
+      float2* crow = C + std::uint64_t(batch) * c_batch_stride + std::uint64_t(m0 + row) * n;
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        std::uint32_t re[32], im[32];
+        const std::uint32_t base = tmem + (std::uint32_t(q * 32) << 16);
+        TMEM_LD32(base + c0, re);
+        TMEM_LD32(base + BN + c0, im);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (m0 + row < m) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int col = n0 + c0 + j;
+            if (col < n) crow[col] = make_float2(__uint_as_float(re[j]), __uint_as_float(im[j]));
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 1) {
+    // If the pipeline was abandoned, give the tensor core time to finish the
+    // MMAs already issued before the accumulator is released.
+    if (*abort_flag) {
+      const unsigned long long t0 = now_ns();
+      while (!mbar_test(tmem_full, 0) && now_ns() - t0 < WAIT_NS) {
+      }
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+  }
+}
+
+// Splits complex64 rows into the four TF32 planes (round-to-nearest).
+__device__ __forceinline__ float tf32_rn(float x) {
+  std::uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__global__ void __launch_bounds__(256) split_tf32_kernel(const float2* __restrict__ src, float* __restrict__ planes,
+                                                         std::uint64_t count, std::uint64_t src_batch_stride) {
+  const std::uint64_t b = blockIdx.y;
+  const float2* s = src + b * src_batch_stride;
+  float* p = planes + b * 4 * count;
+  for (std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count;
+       i += std::uint64_t(gridDim.x) * blockDim.x) {
+    const float2 v = s[i];
+    const float rh = tf32_rn(v.x), ih = tf32_rn(v.y);
+    p[i] = rh;
+    p[count + i] = tf32_rn(v.x - rh);
+    p[2 * count + i] = ih;
+    p[3 * count + i] = tf32_rn(v.y - ih);
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  if (!fn) throw std::string("ERROR (qflex_gb300: tensor cores) --> cuTensorMapEncodeTiled unavailable");
+  return fn;
+}
+
+// 4-D map over planes laid out [batch][4][rows][k] (fp32), box
+// {BK, box_rows, 4, 1}, 32-byte swizzle.
+CUtensorMap plane_map(const float* base, std::uint64_t rows, std::uint64_t k, int batch, int box_rows) {
+  CUtensorMap map;
+  std::memset(&map, 0, sizeof(map));
+  const cuuint64_t dims[4] = {k, rows, 4, (cuuint64_t)batch};
+  const cuuint64_t strides[3] = {k * 4, rows * k * 4, 4 * rows * k * 4};
+  const cuuint32_t box[4] = {BK, (cuuint32_t)box_rows, 4, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(base), dims, strides,
+                           box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    throw std::string("ERROR (qflex_gb300: tensor cores) --> cuTensorMapEncodeTiled failed: ") +
+        std::to_string((int)r);
+  return map;
+}
+
+void check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw std::string("ERROR (qflex_gb300: CUDA ") + what + ") --> " + cudaGetErrorString(e);
+}
+
+}  // namespace
+
+bool tc_eligible(std::size_t m, std::size_t n, std::size_t k) {
+  return m >= 64 && n >= 64 && k >= 16 && k % 4 == 0 && m < (1u << 31) && n < (1u << 31) && k < (1u << 31);
+}
+
+std::size_t tc_workspace_elems(std::size_t m, std::size_t n, std::size_t k) { return 4 * (m + n) * k; }
+
+void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size_t m, std::size_t n,
+                         std::size_t k, std::uint64_t batch_stride, std::uint64_t bt_stride, int batch,
+                         float* workspace, int* err, cudaStream_t s) {
+  if (!tc_eligible(m, n, k)) throw std::string("ERROR (qflex_gb300: tensor cores) --> shape not eligible");
+  static bool attr = false;
+  if (!attr) {
+    check(cudaFuncSetAttribute(cgemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
+          "cudaFuncSetAttribute");
+    attr = true;
+  }
+  float* pa = workspace;
+  float* pb = workspace + 4 * m * k * (std::size_t)batch;
+  {
+    dim3 ga((unsigned)std::min<std::uint64_t>((m * k + 255) / 256, 152 * 16), (unsigned)batch);
+    split_tf32_kernel<<<ga, 256, 0, s>>>(A, pa, m * k, batch_stride);
+    dim3 gb((unsigned)std::min<std::uint64_t>((n * k + 255) / 256, 152 * 16), (unsigned)batch);
+    split_tf32_kernel<<<gb, 256, 0, s>>>(Bt, pb, n * k, bt_stride);
+    check(cudaGetLastError(), "split_tf32");
+  }
+  const CUtensorMap ma = plane_map(pa, m, k, batch, BM);
+  const CUtensorMap mb = plane_map(pb, n, k, batch, BN);
+  const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
+  dim3 grid((unsigned)tiles, 1, (unsigned)batch);
+  cgemm_tf32x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err);
+  check(cudaGetLastError(), "cgemm_tf32x3");
+}
+
+}  // namespace qfx

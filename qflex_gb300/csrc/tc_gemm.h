@@ -1,0 +1,26 @@
+// Split-precision complex64 products on the tcgen05 tensor cores.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace qfx {
+
+// Shapes the tensor-core kernel takes (k a multiple of 4 for the TMA row
+// stride; smaller products stay on the CUDA-core kernels).
+bool tc_eligible(std::size_t m, std::size_t n, std::size_t k);
+// fp32 elements of split planes one batch entry needs (A and B, 4 planes).
+std::size_t tc_workspace_elems(std::size_t m, std::size_t n, std::size_t k);
+
+// C[m,n] = A[m,k] * Bt[n,k]^T (complex64, both K-major), 3xTF32 split,
+// FP32 accumulation. Batch entry b reads A + b * ac_stride,
+// Bt + b * bt_stride and writes C + b * ac_stride. `workspace` holds
+// batch * tc_workspace_elems fp32; `err` (device int) receives a nonzero
+// code if a pipeline wait expired.
+void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size_t m, std::size_t n,
+                         std::size_t k, std::uint64_t ac_stride, std::uint64_t bt_stride, int batch,
+                         float* workspace, int* err, cudaStream_t s);
+
+}  // namespace qfx

@@ -200,6 +200,6 @@ def test_simulate_drop_in(built_lib, ref_cases, capsys):
     # Errors print and return [] (src/pybind_main.cpp:127-137).
     bad = simulate({"circuit": case["circuit"].splitlines(), "ordering": case["ordering"].splitlines(),
                     "grid": case["grid"].splitlines(), "initial_state": "00000", "final_state": "1100x",
-                    "memory_limit": "1KB"})
+                    "memory_limit": 512})  # the plan needs 832 bytes
     assert bad == []
     assert "exceeds memory limit" in capsys.readouterr().err

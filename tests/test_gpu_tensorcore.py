@@ -1,0 +1,71 @@
+"""Split-precision (3xTF32) tcgen05 products and the engine in that mode.
+Tolerance: per-amplitude error within 1e-5 of the RMS amplitude against
+the reference's complex<float> results and the FP64 oracle; products within
+4e-6 of the FP64 product (relative to sqrt(k) for unit-variance data)."""
+import numpy as np
+import pytest
+
+from oracle import qflex_oracle as qo
+from qflex_gb300 import TF32X3, Context, rqc
+from tests.conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def tc_ctx(built_lib):
+    return Context(0, TF32X3)
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 128, 16), (64, 64, 16), (256, 512, 128), (1024, 256, 256),
+                                   (300, 128, 64), (128, 1024, 40), (4096, 256, 256)])
+def test_tf32x3_multiply(tc_ctx, m, n, k):
+    import torch
+    g = np.random.default_rng(m + 7 * n + 13 * k)
+    A = (g.standard_normal((m, k)) + 1j * g.standard_normal((m, k))).astype(np.complex64)
+    B = (g.standard_normal((k, n)) + 1j * g.standard_normal((k, n))).astype(np.complex64)
+    dA, dB = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+    dC = torch.full((m, n), float("nan"), dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()
+    tc_ctx.multiply(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), m, n, k)
+    tc_ctx.synchronize()
+    got = dC.cpu().numpy()
+    want = A.astype(np.complex128) @ B.astype(np.complex128)
+    err = np.max(np.abs(got - want)) / np.sqrt(k)
+    assert np.isfinite(got).all()
+    assert err < 4e-6, err
+
+
+ENGINE_CASES = ["c1_4x5_d16", "rect4x4_cut_terminal", "c2_6x6_d24_partial_cut", "fsim_3x4_off",
+                "c3_7x7_d32_one_slice"]
+
+
+@pytest.mark.parametrize("name", ENGINE_CASES)
+def test_tf32x3_engine_matches_reference(tc_ctx, ref_cases, name):
+    case = ref_cases[name]
+    limit = qo.parse_memory(case["memory_limit"])
+    finals = [r["final"] for r in case["runs"]]
+    out = tc_ctx.evaluate_many(case["circuit"], case["ordering"], case["grid"], case["initial"], finals,
+                               limit)
+    want = [complex(*a) for r in case["runs"] for a in r["amplitudes"]]
+    assert [s for s, _ in out] == [s for r in case["runs"] for s in r["states"]]
+    assert rel_err([a for _, a in out], want) < TOL, name
+
+
+def test_tf32x3_plan_uses_tensor_cores(tc_ctx, ref_cases):
+    case = ref_cases["c3_7x7_d32_one_slice"]
+    tc_ctx.evaluate(case["circuit"], case["ordering"], case["grid"], "", "", 1 << 40)
+    plan = Context(-1, TF32X3)
+    plan.evaluate(case["circuit"], case["ordering"], case["grid"], "", "", 1 << 40)
+    assert plan.gemms() == [tuple(g) for g in case["runs"][0]["gemms"]]
+
+
+def test_tf32x3_vs_fp64_oracle_c1(tc_ctx):
+    c, o, g, ini, fins = rqc.workload("c1", seed=8)
+    out = tc_ctx.evaluate_many(c, o, g, ini, fins[:4])
+    want = []
+    for f in fins[:4]:
+        inp = qo.Input(qo.Circuit.loads(c), qo.load_ordering(o), qo.Grid.loads(g), ini, f)
+        want.append(qo.evaluate_circuit(inp, np.complex128)[0][1])
+    assert rel_err([a for _, a in out], want) < TOL
