@@ -138,6 +138,29 @@ int qflex_gb300_multiply(qflex_gb300_context* ctx, const void* A, const void* B,
 
 int qflex_gb300_synchronize(qflex_gb300_context* ctx);
 
+/* Skinny product that allocates no device memory: C[m,n] = A[m,k] * B[k,n]
+ * (row-major complex64) for at most 64 outputs (m * n <= 64, m, n <= 64),
+ * i.e. the dot products and narrow matrix-vector products that multiply()
+ * hands to cblas_cgemv / cblas_cdotu_sub. This one has no counterpart in
+ * the reference: it exists for callers that must not allocate, because
+ * cudaMalloc / cudaFree may synchronize the whole device or the caller has
+ * no memory budget left to give. It takes no context; work is queued on
+ * `stream` (a cudaStream_t, NULL for the legacy stream) of the current
+ * device.
+ *
+ * The split-k partial sums go to one fixed array of 65536 complex64 slots
+ * (512 KiB) compiled into the library; every GPU that loads the library
+ * holds it until the process exits. The first call made with a device
+ * current looks up that device's copy of the array (cudaGetSymbolAddress);
+ * make that first call before any stream capture. All calls share the
+ * array: calls that overlap on the GPU (other streams, other threads) race
+ * and corrupt each other's results, so serialize them. Every slot a call
+ * reads is written by that call first, so nothing needs clearing. Sizes
+ * beyond the limits return QFLEX_GB300_ERR_ARG with a message in `err`
+ * (`err_len` bytes, may be NULL). */
+int qflex_gb300_multiply_skinny_noalloc(const void* A, const void* B, void* C, size_t m, size_t n,
+                                        size_t k, void* stream, char* err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,7 +25,7 @@ EXPORTS = (
     "qflex_gb300_result_final_state", "qflex_gb300_last_stats", "qflex_gb300_last_shapes",
     "qflex_gb300_last_gemms", "qflex_gb300_permute", "qflex_gb300_check_permute",
     "qflex_gb300_reorder",
-    "qflex_gb300_multiply", "qflex_gb300_synchronize",
+    "qflex_gb300_multiply", "qflex_gb300_synchronize", "qflex_gb300_multiply_skinny_noalloc",
 )
 
 
@@ -90,6 +90,7 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
             "qflex_gb300_reorder": (i, [vp, vp, vp, sz, C.POINTER(sz), C.POINTER(sz)]),
             "qflex_gb300_multiply": (i, [vp, vp, vp, vp, sz, sz, sz, sz, sz]),
             "qflex_gb300_synchronize": (i, [vp]),
+            "qflex_gb300_multiply_skinny_noalloc": (i, [vp, vp, vp, sz, sz, sz, vp, C.c_char_p, sz]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -112,6 +113,18 @@ def check_permute(src, dims: Sequence[int], new_order: Sequence[int]):
     if rc != OK:
         raise QflexGb300Error(rc, "permutation schedule check failed")
     return out
+
+
+def multiply_skinny_noalloc(A: int, B: int, Cp: int, m: int, n: int, k: int, stream: int = 0) -> None:
+    """C[m,n] = A[m,k] * B[k,n] for at most 64 outputs, without allocating
+    device memory (see qflex_gb300_multiply_skinny_noalloc). Pointers are
+    CUDA device addresses; `stream` a cudaStream_t handle (0: legacy)."""
+    lib = load_library()
+    err = C.create_string_buffer(512)
+    rc = lib.qflex_gb300_multiply_skinny_noalloc(C.c_void_p(A), C.c_void_p(B), C.c_void_p(Cp), m, n, k,
+                                                 C.c_void_p(stream or None), err, len(err))
+    if rc != OK:
+        raise QflexGb300Error(rc, err.value.decode())
 
 
 def _b(s: Optional[str]) -> bytes:

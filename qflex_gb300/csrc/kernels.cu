@@ -474,6 +474,17 @@ int skinny_splits(std::size_t m, std::size_t n, std::size_t k, int batch) {
   return splits >= 2 ? (int)splits : 0;
 }
 
+void launch_skinny_split(const float2* A, const float2* B, float2* C, std::size_t m, std::size_t n,
+                        std::size_t k, int splits, float2* partial, cudaStream_t s) {
+  const int outputs = (int)(m * n);
+  dim3 g1((unsigned)(outputs * splits), 1u);
+  skinny_partial<<<g1, 256, 0, s>>>(A, B, partial, (int)n, k, splits, 0);
+  check_launch("skinny_partial");
+  dim3 g2((unsigned)((outputs * 32 + 127) / 128), 1u);
+  skinny_finish<<<g2, 128, 0, s>>>(partial, C, outputs, splits, 0);
+  check_launch("skinny_finish");
+}
+
 void launch_cgemm_fp32(const float2* A, const float2* B, float2* C, std::size_t m, std::size_t n,
                        std::size_t k, std::uint64_t stride, int batch, cudaStream_t s,
                        float2* scratch) {

@@ -83,6 +83,12 @@ void launch_cgemm_fp32(const float2* A, const float2* B, float2* C, std::size_t 
                        std::size_t k, std::uint64_t batch_stride, int batch, cudaStream_t s,
                        float2* scratch);
 
+// One skinny product (m * n outputs) with k split over `splits` blocks per
+// output; `partial` holds m * n * splits float2, every one of which is
+// written before it is read.
+void launch_skinny_split(const float2* A, const float2* B, float2* C, std::size_t m, std::size_t n,
+                        std::size_t k, int splits, float2* partial, cudaStream_t s);
+
 // ---- FP64 amplitude sums -------------------------------------------------------
 // amps[b * n_amps + a] += sum of results[b * stride + leaf] over the leaves
 // of amplitude a (CSR: leaves[ptr[a] .. ptr[a+1])), in leaf order.
