@@ -38,12 +38,14 @@ struct Engine::Plan {
   ColumnDesc* d_cols = nullptr;
   StepDesc* d_steps = nullptr;
   float2* d_mats = nullptr;
+  float2* d_mats_lo = nullptr;  // null: plain FP32 columns
   std::uint32_t* d_ptr = nullptr;
   std::uint32_t* d_leaves = nullptr;
   ~Plan() {
     cudaFree(d_cols);
     cudaFree(d_steps);
     cudaFree(d_mats);
+    cudaFree(d_mats_lo);
     cudaFree(d_ptr);
     cudaFree(d_leaves);
   }
@@ -181,8 +183,9 @@ namespace {
 
 // Flatten descriptors: where each column's 2D tensor lives and which bit of
 // its element index each two-qubit half reads.
-void build_flatten_tables(const Network& net, const Program& prog, std::vector<ColumnDesc>* cols,
-                          std::vector<StepDesc>* steps, std::vector<float2>* mats,
+void build_flatten_tables(const Network& net, const Program& prog, bool exact_gates,
+                          std::vector<ColumnDesc>* cols, std::vector<StepDesc>* steps,
+                          std::vector<float2>* mats, std::vector<float2>* mats_lo,
                           std::uint32_t* max_log2) {
   *max_log2 = 0;
   for (std::size_t c = 0; c < net.columns.size(); ++c) {
@@ -220,7 +223,16 @@ void build_flatten_tables(const Network& net, const Program& prog, std::vector<C
         }
         sd.shift = (std::uint32_t)shift;
       }
-      for (const auto& z : s.data) mats->push_back(make_float2(z.real(), z.imag()));
+      if (exact_gates) {
+        // hi + lo of each double-precision constant
+        for (const auto& z : s.exact) {
+          const float hr = float(z.real()), hi = float(z.imag());
+          mats->push_back(make_float2(hr, hi));
+          mats_lo->push_back(make_float2(float(z.real() - double(hr)), float(z.imag() - double(hi))));
+        }
+      } else {
+        for (const auto& z : s.data) mats->push_back(make_float2(z.real(), z.imag()));
+      }
       steps->push_back(sd);
     }
     cd.step_end = (std::uint32_t)steps->size();
@@ -308,8 +320,11 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
         make_perm_plan(p.prog.ops[i].nbits, p.prog.ops[i].perm, &p.perm[i]);
     std::vector<ColumnDesc> cols;
     std::vector<StepDesc> steps;
-    std::vector<float2> mats;
-    build_flatten_tables(p.net, p.prog, &cols, &steps, &mats, &p.max_size_log2);
+    std::vector<float2> mats, mats_lo;
+    // The plain FP32 path keeps the reference's float gate constants; the
+    // split-precision path evaluates the columns from double constants.
+    const bool exact_gates = precision_ != FP32;
+    build_flatten_tables(p.net, p.prog, exact_gates, &cols, &steps, &mats, &mats_lo, &p.max_size_log2);
     std::vector<std::uint32_t> ptr(p.prog.n_amplitudes + 1, 0), leaves(p.prog.n_leaves);
     for (std::size_t l = 0; l < p.prog.n_leaves; ++l) ++ptr[p.prog.leaf_amp[l] + 1];
     for (std::size_t a = 0; a < p.prog.n_amplitudes; ++a) ptr[a + 1] += ptr[a];
@@ -319,6 +334,7 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
       p.d_cols = upload(cols);
       p.d_steps = upload(steps);
       p.d_mats = upload(mats);
+      if (exact_gates) p.d_mats_lo = upload(mats_lo);
       p.d_ptr = upload(ptr);
       p.d_leaves = upload(leaves);
     }
@@ -399,7 +415,7 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
     QFX_CUDA(cudaMemcpyAsync(d_bits, bits.data(), bits.size(), cudaMemcpyHostToDevice, stream_));
     QFX_CUDA(cudaMemsetAsync(d_amps, 0, std::max<std::size_t>(n_amps, 1) * sizeof(double2) * nb, stream_));
     QFX_CUDA(cudaEventRecord(ev0_, stream_));
-    launch_flatten(p.d_cols, (int)n_cols, p.max_size_log2, p.d_steps, p.d_mats, d_bits,
+    launch_flatten(p.d_cols, (int)n_cols, p.max_size_log2, p.d_steps, p.d_mats, p.d_mats_lo, d_bits,
                    d_bits + n_cols * (std::size_t)nb, arena, prog.arena_elems, nb, stream_);
     run_program(p, nb, arena, tc_ws);
     launch_reduce_amplitudes(arena + prog.results_offset, prog.arena_elems, p.d_ptr, p.d_leaves,

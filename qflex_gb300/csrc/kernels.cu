@@ -31,9 +31,52 @@ void check_launch(const char* what) {
 // ---------------------------------------------------------------------------
 // Column flatten.
 // ---------------------------------------------------------------------------
+// Float-float numbers (an unevaluated sum h + l of two floats, ~44
+// significant bits) built from the classic error-free transformations:
+// Knuth's two-sum and the FMA-based exact product.
+struct ff {
+  float h, l;
+};
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  const float s = a.h + b.h;
+  const float bb = s - a.h;
+  float e = (a.h - (s - bb)) + (b.h - bb);
+  e += a.l + b.l;
+  const float h = s + e;
+  return {h, e - (h - s)};
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  const float h = p + e;
+  return {h, e - (h - p)};
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return {-a.h, -a.l}; }
+struct cff {
+  ff re, im;
+};
+__device__ __forceinline__ cff cff_mul(cff a, cff b) {
+  return {ff_add(ff_mul(a.re, b.re), ff_neg(ff_mul(a.im, b.im))),
+          ff_add(ff_mul(a.re, b.im), ff_mul(a.im, b.re))};
+}
+__device__ __forceinline__ cff cff_add(cff a, cff b) { return {ff_add(a.re, b.re), ff_add(a.im, b.im)}; }
+__device__ __forceinline__ cff cff_load(const float2* hi, const float2* lo, std::uint32_t i) {
+  const float2 h = __ldg(hi + i), l = __ldg(lo + i);
+  return {{h.x, l.x}, {h.y, l.y}};
+}
+
+// Element e of a column's 2D tensor: <final| G_K ... G_1 |init> with every
+// two-qubit half reading its virtual digit of e. Plain FP32 repeats the
+// reference's complex<float> arithmetic on its float gate constants; the
+// compensated form carries float-float values and gate constants (hi + lo
+// of the double-precision gate) and rounds once at the end.
+template <bool kCompensated>
 __global__ void __launch_bounds__(256) flatten_kernel(const ColumnDesc* __restrict__ cols,
                                                       const StepDesc* __restrict__ steps,
                                                       const float2* __restrict__ mats,
+                                                      const float2* __restrict__ mats_lo,
                                                       const std::uint8_t* __restrict__ init_bits,
                                                       const std::uint8_t* __restrict__ final_bits,
                                                       int n_cols, float2* __restrict__ arena,
@@ -43,24 +86,35 @@ __global__ void __launch_bounds__(256) flatten_kernel(const ColumnDesc* __restri
   const ColumnDesc cd = cols[c];
   const std::uint64_t e = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= (std::uint64_t(1) << cd.size_log2)) return;
-  float2 p0 = make_float2(1.f, 0.f), p1 = make_float2(0.f, 0.f);
-  if (init_bits[std::size_t(b) * n_cols + c]) {
-    p0 = make_float2(0.f, 0.f);
-    p1 = make_float2(1.f, 0.f);
-  }
+  const bool one = init_bits[std::size_t(b) * n_cols + c] != 0;
+  float2 p0 = make_float2(one ? 0.f : 1.f, 0.f), p1 = make_float2(one ? 1.f : 0.f, 0.f);
+  cff f0 = {{p0.x, 0.f}, {0.f, 0.f}}, f1 = {{p1.x, 0.f}, {0.f, 0.f}};
   for (std::uint32_t s = cd.step_begin; s < cd.step_end; ++s) {
     const StepDesc sd = steps[s];
-    const float2* g = mats + sd.mat;
+    std::uint32_t g = sd.mat;
     std::uint32_t row = 2;  // distance between input rows of the gate data
     if (sd.kind == 2) {
       const std::uint32_t v = std::uint32_t(e >> sd.shift) & (sd.V - 1);
       g += 2 * v;
       row = 2 * sd.V;
     }
-    const float2 q0 = cfma(p1, __ldg(g + row), cmul(p0, __ldg(g)));
-    const float2 q1 = cfma(p1, __ldg(g + row + 1), cmul(p0, __ldg(g + 1)));
-    p0 = q0;
-    p1 = q1;
+    if constexpr (kCompensated) {
+      const cff q0 = cff_add(cff_mul(f0, cff_load(mats, mats_lo, g)),
+                             cff_mul(f1, cff_load(mats, mats_lo, g + row)));
+      const cff q1 = cff_add(cff_mul(f0, cff_load(mats, mats_lo, g + 1)),
+                             cff_mul(f1, cff_load(mats, mats_lo, g + row + 1)));
+      f0 = q0;
+      f1 = q1;
+    } else {
+      const float2 q0 = cfma(p1, __ldg(mats + g + row), cmul(p0, __ldg(mats + g)));
+      const float2 q1 = cfma(p1, __ldg(mats + g + row + 1), cmul(p0, __ldg(mats + g + 1)));
+      p0 = q0;
+      p1 = q1;
+    }
+  }
+  if constexpr (kCompensated) {
+    p0 = make_float2(f0.re.h + f0.re.l, f0.im.h + f0.im.l);
+    p1 = make_float2(f1.re.h + f1.re.l, f1.im.h + f1.im.l);
   }
   int bit;
   if (cd.o_shift >= 0)
@@ -362,14 +416,18 @@ void run_cgemm(const float2* A, const float2* B, float2* C, std::size_t m, std::
 }  // namespace
 
 void launch_flatten(const ColumnDesc* cols, int n_cols, std::uint32_t max_size_log2,
-                    const StepDesc* steps, const float2* mats, const std::uint8_t* init_bits,
-                    const std::uint8_t* final_bits, float2* arena, std::uint64_t arena_stride,
-                    int batch, cudaStream_t s) {
+                    const StepDesc* steps, const float2* mats, const float2* mats_lo,
+                    const std::uint8_t* init_bits, const std::uint8_t* final_bits, float2* arena,
+                    std::uint64_t arena_stride, int batch, cudaStream_t s) {
   if (n_cols == 0) return;
   const std::uint64_t blocks = ((std::uint64_t(1) << max_size_log2) + 255) / 256;
   dim3 grid((unsigned)blocks, (unsigned)n_cols, (unsigned)batch);
-  flatten_kernel<<<grid, 256, 0, s>>>(cols, steps, mats, init_bits, final_bits, n_cols, arena,
-                                      arena_stride);
+  if (mats_lo)
+    flatten_kernel<true><<<grid, 256, 0, s>>>(cols, steps, mats, mats_lo, init_bits, final_bits, n_cols,
+                                              arena, arena_stride);
+  else
+    flatten_kernel<false><<<grid, 256, 0, s>>>(cols, steps, mats, mats, init_bits, final_bits, n_cols,
+                                               arena, arena_stride);
   check_launch("flatten");
 }
 

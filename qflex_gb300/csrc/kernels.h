@@ -26,10 +26,13 @@ struct StepDesc {
   std::uint32_t mat;      // offset of the gate data in the matrix pool
 };
 
+// `mats` holds the gate data as complex64; with `mats_lo` (the remainders
+// of the double-precision gates) the chains run in float-float arithmetic,
+// otherwise in plain FP32 like the reference.
 void launch_flatten(const ColumnDesc* cols, int n_cols, std::uint32_t max_size_log2,
-                    const StepDesc* steps, const float2* mats, const std::uint8_t* init_bits,
-                    const std::uint8_t* final_bits, float2* arena, std::uint64_t arena_stride,
-                    int batch, cudaStream_t s);
+                    const StepDesc* steps, const float2* mats, const float2* mats_lo,
+                    const std::uint8_t* init_bits, const std::uint8_t* final_bits, float2* arena,
+                    std::uint64_t arena_stride, int batch, cudaStream_t s);
 
 // ---- index permutation over binary digits --------------------------------------
 // The tensor is viewed as nbits binary digits; input digit p moves to output

@@ -153,61 +153,67 @@ namespace {
 
 using cfloat = std::complex<float>;
 
-// Gate constants of src/read_circuit.cpp:27-79, stored as complex64 like the
-// reference's s_type. One-qubit gates are (input, output); two-qubit halves
-// are (input, virtual, output).
-const std::unordered_map<std::string, std::vector<cfloat>>& gate_table() {
-  static const float r = static_cast<float>(M_SQRT1_2);
-  static const std::unordered_map<std::string, std::vector<cfloat>> t = {
-      {"h", {r, r, r, -r}},
-      {"hz_1_2", {{0.5f, 0.5f}, {r, 0.f}, {0.f, -r}, {0.5f, 0.5f}}},
-      {"t", {1.f, 0.f, 0.f, {r, r}}},
-      {"x_1_2", {{0.5f, 0.5f}, {0.5f, -0.5f}, {0.5f, -0.5f}, {0.5f, 0.5f}}},
-      {"y_1_2", {{0.5f, 0.5f}, {0.5f, 0.5f}, {-0.5f, -0.5f}, {0.5f, 0.5f}}},
-      {"cz_q1",
-       {float(-0.3446133714352872), 0.f, float(1.1381806476131544), 0.f, 0.f,
-        float(-1.1381806476131544), 0.f, float(-0.3446133714352872)}},
-      {"cz_q2",
-       {float(-1.0484937059720079), 0.f, float(0.5611368023131075), 0.f, 0.f,
-        float(0.5611368023131075), 0.f, float(1.0484937059720079)}},
-      {"cx_q1",
-       {float(0.8408964152537143), 0.f, float(0.8408964152537143), 0.f, 0.f,
-        float(-0.8408964152537143), 0.f, float(0.8408964152537143)}},
-      {"cx_q2",
-       {float(0.5946035575013604), float(-0.5946035575013604), float(0.5946035575013604),
-        float(0.5946035575013604), float(-0.5946035575013604), float(0.5946035575013604),
-        float(0.5946035575013604), float(0.5946035575013604)}},
-  };
+// Gate constants of src/read_circuit.cpp:27-79. One-qubit gates are
+// (input, output); two-qubit halves are (input, virtual, output). With
+// T = float the values are exactly the reference's complex64 constants; with
+// T = double they are the same constants in double (the split-precision path
+// evaluates the time columns with these).
+template <typename T>
+std::vector<std::complex<T>> table_gate(const std::string& name) {
+  using C = std::complex<T>;
+  const T r = static_cast<T>(M_SQRT1_2), h = T(0.5);
+  auto v = [](double x) { return C(static_cast<T>(x), T(0)); };
+  if (name == "h") return {C(r), C(r), C(r), C(-r)};
+  if (name == "hz_1_2") return {C(h, h), C(r, 0), C(0, -r), C(h, h)};
+  if (name == "t") return {C(1), C(0), C(0), C(r, r)};
+  if (name == "x_1_2") return {C(h, h), C(h, -h), C(h, -h), C(h, h)};
+  if (name == "y_1_2") return {C(h, h), C(h, h), C(-h, -h), C(h, h)};
+  if (name == "cz_q1")
+    return {v(-0.3446133714352872), v(0), v(1.1381806476131544), v(0), v(0), v(-1.1381806476131544), v(0),
+            v(-0.3446133714352872)};
+  if (name == "cz_q2")
+    return {v(-1.0484937059720079), v(0), v(0.5611368023131075), v(0), v(0), v(0.5611368023131075), v(0),
+            v(1.0484937059720079)};
+  if (name == "cx_q1")
+    return {v(0.8408964152537143), v(0), v(0.8408964152537143), v(0), v(0), v(-0.8408964152537143), v(0),
+            v(0.8408964152537143)};
+  if (name == "cx_q2") {
+    const T a = static_cast<T>(0.5946035575013604);
+    return {C(a), C(-a), C(a), C(a), C(-a), C(a), C(a), C(a)};
+  }
+  return {};
+}
+
+template <typename T>
+std::vector<std::complex<T>> one_qubit_gate(const Gate& g) {
+  using C = std::complex<T>;
+  if (g.name == "rz") {
+    // rz(x) = diag(conj(p), p), p = exp(i * pi * x / 2); the reference
+    // evaluates it in float (src/read_circuit.cpp:84-88).
+    const double angle = M_PI * g.params.at(0);
+    const C phase = std::exp(C(T(0), static_cast<T>(angle / 2)));
+    return {std::conj(phase), C(0), C(0), phase};
+  }
+  auto t = table_gate<T>(g.name);
+  if (t.size() != 4) throw QFX_ERR("Invalid gate name provided: ", g.name);
   return t;
 }
 
-std::vector<cfloat> one_qubit_gate(const Gate& g) {
-  if (g.name == "rz") {
-    // rz(x) = diag(conj(p), p), p = exp(i * pi * x / 2), evaluated in float
-    // (src/read_circuit.cpp:84-88).
-    const double angle = M_PI * g.params.at(0);
-    const cfloat phase = std::exp(cfloat(0.f, static_cast<float>(angle / 2)));
-    return {std::conj(phase), 0.f, 0.f, phase};
-  }
-  auto it = gate_table().find(g.name);
-  if (it == gate_table().end() || it->second.size() != 4)
-    throw QFX_ERR("Invalid gate name provided: ", g.name);
-  return it->second;
-}
-
 // fSim(theta, phi) split into two identical (input, virtual[4], output)
-// halves, angles in units of pi; arithmetic in float as in
-// src/read_circuit.cpp:105-139,156-162.
-std::vector<cfloat> fsim_half(double theta_pi, double phi_pi) {
-  const float th = static_cast<float>(M_PI * theta_pi);
-  const float ph = static_cast<float>(M_PI * phi_pi);
-  const cfloat e = std::exp(cfloat(0.f, -1 * ph / 2));
-  const cfloat c1 = cfloat(0.5f) * (e + cfloat(std::cos(th), 0.f));
-  const cfloat c2 = cfloat(0.5f) * (e - cfloat(std::cos(th), 0.f));
-  const cfloat c3 = cfloat(0.f, float(-1 / 2.)) * cfloat(std::sin(th), 0.f);
-  const cfloat s1 = std::sqrt(c1), s2 = std::sqrt(c2), s3 = std::sqrt(c3), s4 = std::sqrt(c3);
-  const cfloat d = std::exp(cfloat(0.f, float(ph / 4.)));
-  const cfloat z(0.f, 0.f), I(0.f, 1.f);
+// halves, angles in units of pi (src/read_circuit.cpp:105-139,156-162);
+// T = float repeats the reference's float arithmetic.
+template <typename T>
+std::vector<std::complex<T>> fsim_half(double theta_pi, double phi_pi) {
+  using C = std::complex<T>;
+  const T th = static_cast<T>(M_PI * theta_pi);
+  const T ph = static_cast<T>(M_PI * phi_pi);
+  const C e = std::exp(C(T(0), -1 * ph / 2));
+  const C c1 = C(T(0.5)) * (e + C(std::cos(th), T(0)));
+  const C c2 = C(T(0.5)) * (e - C(std::cos(th), T(0)));
+  const C c3 = C(T(0), static_cast<T>(-1 / 2.)) * C(std::sin(th), T(0));
+  const C s1 = std::sqrt(c1), s2 = std::sqrt(c2), s3 = std::sqrt(c3), s4 = std::sqrt(c3);
+  const C d = std::exp(C(T(0), static_cast<T>(ph / 4.)));
+  const C z(0, 0), I(0, 1);
   return {d * s1, z, d * s2, z, z, s3, z, I * s4,
           z, std::conj(d) * s1, z, -std::conj(d) * s2, s3, z, -I * s4, z};
 }
@@ -344,7 +350,7 @@ Network build_network(const Circuit& circuit, const Grid& grid, const std::strin
     if (g.qubits.size() == 1) {
       Coord c = coords(g.qubits[0]);
       QubitColumn& col = column(c, g.qubits[0]);
-      ColumnStep s{1, 0, -1, 0, one_qubit_gate(g)};
+      ColumnStep s{1, 0, -1, 0, one_qubit_gate<float>(g), one_qubit_gate<double>(g)};
       col.steps.push_back(std::move(s));
     } else if (g.qubits.size() == 2) {
       Coord c1 = coords(g.qubits[0]), c2 = coords(g.qubits[1]);
@@ -353,16 +359,17 @@ Network build_network(const Circuit& circuit, const Grid& grid, const std::strin
       if (std::abs(c1.first - c2.first) + std::abs(c1.second - c2.second) != 1)
         throw QFX_ERR("Qubits ", g.qubits[0], " and ", g.qubits[1], " are not nearest neighbors.");
       std::vector<cfloat> d1, d2;
+      std::vector<std::complex<double>> e1, e2;
       int V = 2;
-      if (g.name == "cz") {
-        d1 = gate_table().at("cz_q1");
-        d2 = gate_table().at("cz_q2");
-      } else if (g.name == "cx") {
-        d1 = gate_table().at("cx_q1");
-        d2 = gate_table().at("cx_q2");
+      if (g.name == "cz" || g.name == "cx") {
+        d1 = table_gate<float>(g.name + "_q1");
+        d2 = table_gate<float>(g.name + "_q2");
+        e1 = table_gate<double>(g.name + "_q1");
+        e2 = table_gate<double>(g.name + "_q2");
       } else if (g.name == "fsim") {
         if (g.params.size() < 2) throw QFX_ERR("fsim needs two parameters: ", g.raw);
-        d1 = d2 = fsim_half(g.params[0], g.params[1]);
+        d1 = d2 = fsim_half<float>(g.params[0], g.params[1]);
+        e1 = e2 = fsim_half<double>(g.params[0], g.params[1]);
         V = 4;
       } else {
         throw QFX_ERR("Invalid gate name provided: ", g.name);
@@ -389,8 +396,8 @@ Network build_network(const Circuit& circuit, const Grid& grid, const std::strin
       }
       const int ordinal = net.links[link].n_gates++;
       net.links[link].V.push_back(V);
-      col1.steps.push_back(ColumnStep{2, V, link, ordinal, d1});
-      col2.steps.push_back(ColumnStep{2, V, link, ordinal, d2});
+      col1.steps.push_back(ColumnStep{2, V, link, ordinal, d1, e1});
+      col2.steps.push_back(ColumnStep{2, V, link, ordinal, d2, e2});
     } else {
       throw QFX_ERR("k-qubit gates with k > 2 not yet implemented.");
     }

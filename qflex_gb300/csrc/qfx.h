@@ -86,7 +86,8 @@ struct ColumnStep {
   int V;             // virtual dimension (2 for cz/cx, 4 for fsim)
   int link;          // index into Network::links for two-qubit halves
   int ordinal;       // 0-based position of this gate among the link's gates
-  std::vector<std::complex<float>> data;  // 4 or 4*V entries
+  std::vector<std::complex<float>> data;  // 4 or 4*V entries, as the reference stores them
+  std::vector<std::complex<double>> exact;  // the same gate evaluated in double
 };
 
 struct Link {

@@ -8,21 +8,31 @@
 // product keeps the three leading terms of every real product
 // (hi*hi + hi*lo + lo*hi) and the complex product uses four real products:
 //   C_re = Ar Br - Ai Bi,   C_im = Ar Bi + Ai Br,
-// i.e. 12 TF32 MMAs per k-step, accumulated in FP32 in TMEM (C_re in
-// columns [0, BN), C_im in [BN, 2 BN)). The minus sign is the instruction
+// i.e. 12 TF32 MMAs per k-step. The minus sign is the instruction
 // descriptor's negate-A bit.
 //
-// Kernel structure (one 128 x 128 output tile per CTA, 192 threads):
+// Accumulation. The tensor core accumulates in FP32 but rounds toward zero,
+// so a long sum in one TMEM accumulator drifts in proportion to the number
+// of k-steps (measured: 6e-5 relative error at k = 4096). The k range is
+// therefore cut into chunks of CHUNK k-steps; chunk c accumulates from zero
+// in TMEM buffer c % 2 (C_re and C_im, 2 x BN columns) while the epilogue
+// warps add chunk c - 1 into FP32 registers with round-to-nearest. The
+// result is as accurate as FP32 CUDA-core arithmetic.
+//
+// Kernel structure (one 128 x 128 output tile per CTA, 320 threads):
 //   warp 0      TMA producer: one 4-D box per operand and stage brings all
 //               four planes (k-step of 8 fp32 = one 32-byte swizzle row)
 //   warp 1      TMEM allocation and the single MMA-issuing thread
-//   warps 2..5  epilogue: tcgen05.ld of the 128 TMEM lanes -> complex64
+//   warps 2..9  epilogue: warp w owns TMEM lanes 32 (w % 4) .. + 31 and one
+//               half of the columns; it drains every chunk into registers
+//               and finally writes complex64
 // Every mbarrier wait is bounded in time; on expiry the CTA records an
 // error code, stops issuing work, waits (bounded) for what it issued and
 // frees its TMEM before returning.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -38,8 +48,9 @@ constexpr int STAGES = 6;
 constexpr int PLANE_A = BM * BK * 4;                 // bytes of one plane tile
 constexpr int PLANE_B = BN * BK * 4;
 constexpr int STAGE_BYTES = 4 * PLANE_A + 4 * PLANE_B;
-constexpr int TMEM_COLS = 2 * BN;
-constexpr int THREADS = 192;
+constexpr int EPI_WARPS = 8;
+constexpr int TMEM_COLS = 4 * BN;         // two chunk buffers of (re, im)
+constexpr int THREADS = 64 + 32 * EPI_WARPS;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s per wait
 
@@ -135,6 +146,11 @@ __device__ __forceinline__ void umma_commit(std::uint64_t* bar) {
         "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])                                            \
       : "r"(taddr))
 
+__device__ __forceinline__ void mbar_arrive(std::uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <int CHUNK>
 __global__ void __launch_bounds__(THREADS, 1)
     cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                         float2* __restrict__ C, int m, int n, int k, std::uint64_t c_batch_stride,
@@ -144,8 +160,10 @@ __global__ void __launch_bounds__(THREADS, 1)
                                                        ~std::uintptr_t(1023));
   std::uint64_t* full = reinterpret_cast<std::uint64_t*>(smem + STAGES * STAGE_BYTES);
   std::uint64_t* empty = full + STAGES;
-  std::uint64_t* tmem_full = empty + STAGES;
-  std::uint32_t* tmem_slot = reinterpret_cast<std::uint32_t*>(tmem_full + 1);
+  std::uint64_t* acc_full = empty + STAGES;   // [2]: a chunk accumulator is complete
+  std::uint64_t* acc_empty = acc_full + 2;    // [2]: a chunk accumulator was drained
+  std::uint64_t* mma_done = acc_empty + 2;    // every issued MMA has completed
+  std::uint32_t* tmem_slot = reinterpret_cast<std::uint32_t*>(mma_done + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -154,13 +172,18 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int n0 = (blockIdx.x / tiles_m) * BN;
   const int batch = blockIdx.z;
   const int kblocks = (k + BK - 1) / BK;
+  const int chunks = (kblocks + CHUNK - 1) / CHUNK;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(tmem_full, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], EPI_WARPS);
+    }
+    mbar_init(mma_done, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -197,67 +220,93 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer. Planes in a stage: A re_hi, re_lo, im_hi, im_lo, then B.
+    // Chunk c (CHUNK k-steps) accumulates from zero into TMEM buffer c % 2;
+    // the epilogue warps add it into their FP32 registers and free it.
     const std::uint32_t idp = idesc_tf32(BM, BN, false), idn = idesc_tf32(BM, BN, true);
-    const std::uint32_t d_re = tmem, d_im = tmem + BN;
     for (int kb = 0; kb < kblocks; ++kb) {
       const int s = kb % STAGES;
+      const int c = kb / CHUNK, buf = c & 1;
+      const bool first = kb % CHUNK == 0;
+      if (first && c >= 2 && !mbar_wait(&acc_empty[buf], ((c >> 1) - 1) & 1, abort_flag, err, 4)) break;
       if (!mbar_wait(&full[s], (kb / STAGES) & 1, abort_flag, err, 2)) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
+      const std::uint32_t d_re = tmem + buf * 2 * BN, d_im = d_re + BN;
       const std::uint32_t a0 = smem_u32(smem + s * STAGE_BYTES);
       const std::uint32_t b0 = a0 + 4 * PLANE_A;
       const std::uint64_t arh = smem_desc_sw32(a0), arl = smem_desc_sw32(a0 + PLANE_A),
                           aih = smem_desc_sw32(a0 + 2 * PLANE_A), ail = smem_desc_sw32(a0 + 3 * PLANE_A);
       const std::uint64_t brh = smem_desc_sw32(b0), brl = smem_desc_sw32(b0 + PLANE_B),
                           bih = smem_desc_sw32(b0 + 2 * PLANE_B), bil = smem_desc_sw32(b0 + 3 * PLANE_B);
-      const std::uint32_t acc = kb > 0 ? 1u : 0u;
-      umma_tf32(d_re, arh, brh, idp, acc);
-      umma_tf32(d_re, arh, brl, idp, 1);
+      // The small hi*lo terms go first and the two large hi*hi terms last,
+      // so only those two additions round against a large accumulator.
+      const std::uint32_t acc = first ? 0u : 1u;
+      umma_tf32(d_re, arh, brl, idp, acc);
       umma_tf32(d_re, arl, brh, idp, 1);
-      umma_tf32(d_re, aih, bih, idn, 1);
       umma_tf32(d_re, aih, bil, idn, 1);
       umma_tf32(d_re, ail, bih, idn, 1);
-      umma_tf32(d_im, arh, bih, idp, acc);
-      umma_tf32(d_im, arh, bil, idp, 1);
+      umma_tf32(d_re, arh, brh, idp, 1);
+      umma_tf32(d_re, aih, bih, idn, 1);
+      umma_tf32(d_im, arh, bil, idp, acc);
       umma_tf32(d_im, arl, bih, idp, 1);
-      umma_tf32(d_im, aih, brh, idp, 1);
       umma_tf32(d_im, aih, brl, idp, 1);
       umma_tf32(d_im, ail, brh, idp, 1);
+      umma_tf32(d_im, arh, bih, idp, 1);
+      umma_tf32(d_im, aih, brh, idp, 1);
       umma_commit(&empty[s]);
+      if (kb % CHUNK == CHUNK - 1 || kb == kblocks - 1) umma_commit(&acc_full[buf]);
     }
-    umma_commit(tmem_full);
+    umma_commit(mma_done);
   } else if (warp >= 2) {
-    // Epilogue: warp w reads TMEM lanes [32 (w % 4), 32 (w % 4) + 32).
+    // Epilogue: warp w reads TMEM lanes [32 (w % 4), 32 (w % 4) + 32) and one
+    // half of the tile's columns. The tensor core's FP32 accumulation rounds
+    // toward zero; keeping each chunk short and adding the chunks here with
+    // round-to-nearest keeps the product as accurate as FP32 arithmetic.
     const int q = warp % 4;
+    const int half = (warp - 2) / 4;
     const int row = q * 32 + lane;
-    const bool ok = mbar_wait(tmem_full, 0, abort_flag, err, 3);
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    if (ok) {
-      float2* crow = C + std::uint64_t(batch) * c_batch_stride + std::uint64_t(m0 + row) * n;
-      for (int c0 = 0; c0 < BN; c0 += 32) {
-        std::uint32_t re[32], im[32];
-        const std::uint32_t base = tmem + (std::uint32_t(q * 32) << 16);
-        TMEM_LD32(base + c0, re);
-        TMEM_LD32(base + BN + c0, im);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (m0 + row < m) {
+    float tre[BN / 2], tim[BN / 2];
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int col = n0 + c0 + j;
-            if (col < n) crow[col] = make_float2(__uint_as_float(re[j]), __uint_as_float(im[j]));
-          }
-        }
+    for (int j = 0; j < BN / 2; ++j) tre[j] = tim[j] = 0.f;
+    bool ok = true;
+    for (int c = 0; c < chunks; ++c) {
+      const int buf = c & 1;
+      if (!mbar_wait(&acc_full[buf], (c >> 1) & 1, abort_flag, err, 3)) {
+        ok = false;
+        break;
       }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const std::uint32_t base = tmem + (std::uint32_t(q * 32) << 16) + buf * 2 * BN + half * (BN / 2);
+#pragma unroll
+      for (int j0 = 0; j0 < BN / 2; j0 += 32) {
+        std::uint32_t v[32];
+        TMEM_LD32(base + j0, v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 32; ++j) tre[j0 + j] += __uint_as_float(v[j]);
+        TMEM_LD32(base + BN + j0, v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 32; ++j) tim[j0 + j] += __uint_as_float(v[j]);
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[buf]);
+    }
+    if (ok && m0 + row < m) {
+      float2* crow = C + std::uint64_t(batch) * c_batch_stride + std::uint64_t(m0 + row) * n + n0 + half * (BN / 2);
+      const int ncols = n - n0 - half * (BN / 2);
+#pragma unroll
+      for (int j = 0; j < BN / 2; ++j)
+        if (j < ncols) crow[j] = make_float2(tre[j], tim[j]);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   if (warp == 1) {
-    // If the pipeline was abandoned, give the tensor core time to finish the
-    // MMAs already issued before the accumulator is released.
-    if (*abort_flag) {
-      const unsigned long long t0 = now_ns();
-      while (!mbar_test(tmem_full, 0) && now_ns() - t0 < WAIT_NS) {
-      }
+    // Release TMEM only after every MMA this CTA issued has completed (the
+    // wait is immediate unless the pipeline was abandoned).
+    const unsigned long long t0 = now_ns();
+    while (!mbar_test(mma_done, 0) && now_ns() - t0 < WAIT_NS) {
     }
     asm volatile("tcgen05.fence::after_thread_sync;");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
@@ -336,12 +385,23 @@ void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size
                          std::size_t k, std::uint64_t batch_stride, std::uint64_t bt_stride, int batch,
                          float* workspace, int* err, cudaStream_t s) {
   if (!tc_eligible(m, n, k)) throw std::string("ERROR (qflex_gb300: tensor cores) --> shape not eligible");
-  static bool attr = false;
-  if (!attr) {
-    check(cudaFuncSetAttribute(cgemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
+  static const int chunk = [] {
+    // k-steps per TMEM chunk. Measured on the 7x7 (1+32+1) network (8
+    // amplitudes vs FP64): 1 -> max 1.0e-5 at 8.9 amplitudes/s, 2 -> max
+    // 8.7e-6 at 9.8, 4 -> max 1.6e-5 at 10.4. QFLEX_TC_CHUNK overrides 2.
+    const char* e = std::getenv("QFLEX_TC_CHUNK");
+    const int c = e ? std::atoi(e) : 2;
+    return (c == 1 || c == 4) ? c : 2;
+  }();
+  static std::once_flag attr;
+  std::call_once(attr, [] {
+    check(cudaFuncSetAttribute(cgemm_tf32x3_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
           "cudaFuncSetAttribute");
-    attr = true;
-  }
+    check(cudaFuncSetAttribute(cgemm_tf32x3_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
+          "cudaFuncSetAttribute");
+    check(cudaFuncSetAttribute(cgemm_tf32x3_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
+          "cudaFuncSetAttribute");
+  });
   float* pa = workspace;
   float* pb = workspace + 4 * m * k * (std::size_t)batch;
   {
@@ -355,7 +415,12 @@ void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size
   const CUtensorMap mb = plane_map(pb, n, k, batch, BN);
   const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
   dim3 grid((unsigned)tiles, 1, (unsigned)batch);
-  cgemm_tf32x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err);
+  if (chunk == 4)
+    cgemm_tf32x3_kernel<4><<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err);
+  else if (chunk == 2)
+    cgemm_tf32x3_kernel<2><<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err);
+  else
+    cgemm_tf32x3_kernel<1><<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err);
   check(cudaGetLastError(), "cgemm_tf32x3");
 }
 
