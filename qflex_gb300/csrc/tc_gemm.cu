@@ -21,7 +21,8 @@
 //
 // Kernel structure (one 128 x 128 output tile per CTA, 320 threads):
 //   warp 0      TMA producer: one 4-D box per operand and stage brings all
-//               four planes (k-step of 8 fp32 = one 32-byte swizzle row)
+//               four planes of one k-step (8 values per plane side by side
+//               = one 128-byte row per tile row, 128-byte swizzle)
 //   warp 1      TMEM allocation and the single MMA-issuing thread
 //   warps 2..9  epilogue: warp w owns TMEM lanes 32 (w % 4) .. + 31 and one
 //               half of the columns; it drains every chunk into registers
@@ -45,9 +46,12 @@ namespace {
 
 constexpr int BM = 128, BN = 128, BK = 8;
 constexpr int STAGES = 6;
-constexpr int PLANE_A = BM * BK * 4;                 // bytes of one plane tile
-constexpr int PLANE_B = BN * BK * 4;
-constexpr int STAGE_BYTES = 4 * PLANE_A + 4 * PLANE_B;
+// One k-step of an operand tile: every row holds the four planes' 8 values
+// side by side (4 x 32 bytes = one 128-byte row in the 128-byte swizzle),
+// so plane p is the K-major matrix starting 32 p bytes into the tile.
+constexpr int TILE_A = BM * 128;
+constexpr int TILE_B = BN * 128;
+constexpr int STAGE_BYTES = TILE_A + TILE_B;
 constexpr int EPI_WARPS = 8;
 constexpr int TMEM_COLS = 4 * BN;         // two chunk buffers of (re, im)
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
@@ -104,15 +108,16 @@ __device__ __forceinline__ void tma_load_4d(const CUtensorMap* map, std::uint64_
       : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major operand, rows of 32 bytes in the
-// 32-byte swizzle, 8-row groups 256 bytes apart.
-__device__ __forceinline__ std::uint64_t smem_desc_sw32(std::uint32_t addr) {
+// Shared-memory matrix descriptor: K-major operand inside rows of 128 bytes
+// in the 128-byte swizzle (the start address may sit 32, 64 or 96 bytes into
+// the row, as for a K offset), 8-row groups 1024 bytes apart.
+__device__ __forceinline__ std::uint64_t smem_desc_sw128(std::uint32_t addr) {
   std::uint64_t d = 0;
   d |= std::uint64_t((addr & 0x3FFFF) >> 4);       // start address
   d |= std::uint64_t(1) << 16;                     // leading byte offset (unused here)
-  d |= std::uint64_t(256 >> 4) << 32;              // stride byte offset
+  d |= std::uint64_t(1024 >> 4) << 32;             // stride byte offset
   d |= std::uint64_t(1) << 46;                     // descriptor version
-  d |= std::uint64_t(6) << 61;                     // 32-byte swizzle
+  d |= std::uint64_t(2) << 61;                     // 128-byte swizzle
   return d;
 }
 
@@ -150,11 +155,10 @@ __device__ __forceinline__ void mbar_arrive(std::uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-template <int CHUNK>
 __global__ void __launch_bounds__(THREADS, 1)
     cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                         float2* __restrict__ C, int m, int n, int k, std::uint64_t c_batch_stride,
-                        int* __restrict__ err) {
+                        int* __restrict__ err, int CHUNK, int epi_sleep_ns) {
   extern __shared__ __align__(1024) std::uint8_t smem_raw[];
   std::uint8_t* smem = reinterpret_cast<std::uint8_t*>((reinterpret_cast<std::uintptr_t>(smem_raw) + 1023) &
                                                        ~std::uintptr_t(1023));
@@ -167,9 +171,15 @@ __global__ void __launch_bounds__(THREADS, 1)
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  // Tiles run in groups of 8 row-tiles so that the CTAs resident at one
+  // time share A rows and B columns in L2.
   const int tiles_m = (m + BM - 1) / BM;
-  const int m0 = (blockIdx.x % tiles_m) * BM;
-  const int n0 = (blockIdx.x / tiles_m) * BN;
+  const int tiles_n = (n + BN - 1) / BN;
+  const int per_group = 8 * tiles_n;
+  const int group = blockIdx.x / per_group, in_group = blockIdx.x % per_group;
+  const int group_m = min(8, tiles_m - group * 8);
+  const int m0 = (group * 8 + in_group % group_m) * BM;
+  const int n0 = (in_group / group_m) * BN;
   const int batch = blockIdx.z;
   const int kblocks = (k + BK - 1) / BK;
   const int chunks = (kblocks + CHUNK - 1) / CHUNK;
@@ -205,8 +215,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) - 1) & 1, abort_flag, err, 1)) break;
       std::uint8_t* st = smem + s * STAGE_BYTES;
       mbar_expect_tx(&full[s], STAGE_BYTES);
-      tma_load_4d(&map_a, &full[s], st, kb * BK, m0, 0, batch);
-      tma_load_4d(&map_b, &full[s], st + 4 * PLANE_A, kb * BK, n0, 0, batch);
+      tma_load_4d(&map_a, &full[s], st, 0, kb, m0, batch);
+      tma_load_4d(&map_b, &full[s], st + TILE_A, 0, kb, n0, batch);
       issued = kb + 1;
     }
     if (*abort_flag) {
@@ -232,11 +242,11 @@ __global__ void __launch_bounds__(THREADS, 1)
       asm volatile("tcgen05.fence::after_thread_sync;");
       const std::uint32_t d_re = tmem + buf * 2 * BN, d_im = d_re + BN;
       const std::uint32_t a0 = smem_u32(smem + s * STAGE_BYTES);
-      const std::uint32_t b0 = a0 + 4 * PLANE_A;
-      const std::uint64_t arh = smem_desc_sw32(a0), arl = smem_desc_sw32(a0 + PLANE_A),
-                          aih = smem_desc_sw32(a0 + 2 * PLANE_A), ail = smem_desc_sw32(a0 + 3 * PLANE_A);
-      const std::uint64_t brh = smem_desc_sw32(b0), brl = smem_desc_sw32(b0 + PLANE_B),
-                          bih = smem_desc_sw32(b0 + 2 * PLANE_B), bil = smem_desc_sw32(b0 + 3 * PLANE_B);
+      const std::uint32_t b0 = a0 + TILE_A;
+      const std::uint64_t arh = smem_desc_sw128(a0), arl = smem_desc_sw128(a0 + 32),
+                          aih = smem_desc_sw128(a0 + 64), ail = smem_desc_sw128(a0 + 96);
+      const std::uint64_t brh = smem_desc_sw128(b0), brl = smem_desc_sw128(b0 + 32),
+                          bih = smem_desc_sw128(b0 + 64), bil = smem_desc_sw128(b0 + 96);
       // The small hi*lo terms go first and the two large hi*hi terms last,
       // so only those two additions round against a large accumulator.
       const std::uint32_t acc = first ? 0u : 1u;
@@ -270,6 +280,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     bool ok = true;
     for (int c = 0; c < chunks; ++c) {
       const int buf = c & 1;
+      if (epi_sleep_ns > 0)
+        while (!mbar_test(&acc_full[buf], (c >> 1) & 1) && !*abort_flag) __nanosleep(epi_sleep_ns);
       if (!mbar_wait(&acc_full[buf], (c >> 1) & 1, abort_flag, err, 3)) {
         ok = false;
         break;
@@ -278,15 +290,17 @@ __global__ void __launch_bounds__(THREADS, 1)
       const std::uint32_t base = tmem + (std::uint32_t(q * 32) << 16) + buf * 2 * BN + half * (BN / 2);
 #pragma unroll
       for (int j0 = 0; j0 < BN / 2; j0 += 32) {
-        std::uint32_t v[32];
-        TMEM_LD32(base + j0, v);
+        // Both loads in flight before one wait: two TMEM round trips per
+        // chunk instead of four.
+        std::uint32_t vr[32], vi[32];
+        TMEM_LD32(base + j0, vr);
+        TMEM_LD32(base + BN + j0, vi);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int j = 0; j < 32; ++j) tre[j0 + j] += __uint_as_float(v[j]);
-        TMEM_LD32(base + BN + j0, v);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-        for (int j = 0; j < 32; ++j) tim[j0 + j] += __uint_as_float(v[j]);
+        for (int j = 0; j < 32; ++j) {
+          tre[j0 + j] += __uint_as_float(vr[j]);
+          tim[j0 + j] += __uint_as_float(vi[j]);
+        }
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
       __syncwarp();
@@ -320,19 +334,25 @@ __device__ __forceinline__ float tf32_rn(float x) {
   return __uint_as_float(r);
 }
 
+// Output layout per batch entry: [row][k / 8][plane][8] fp32 with planes
+// re_hi, re_lo, im_hi, im_lo; k is padded to a multiple of 8 with zeros.
 __global__ void __launch_bounds__(256) split_tf32_kernel(const float2* __restrict__ src, float* __restrict__ planes,
-                                                         std::uint64_t count, std::uint64_t src_batch_stride) {
+                                                         std::uint64_t rows, std::uint64_t k, std::uint64_t kpad,
+                                                         std::uint64_t src_batch_stride) {
   const std::uint64_t b = blockIdx.y;
-  const float2* s = src + b * src_batch_stride;
-  float* p = planes + b * 4 * count;
+  const float2* sb = src + b * src_batch_stride;
+  float* pb = planes + b * 4 * rows * kpad;
+  const std::uint64_t count = rows * kpad;
   for (std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count;
        i += std::uint64_t(gridDim.x) * blockDim.x) {
-    const float2 v = s[i];
+    const std::uint64_t row = i / kpad, kk = i % kpad;
+    const float2 v = kk < k ? sb[row * k + kk] : make_float2(0.f, 0.f);
     const float rh = tf32_rn(v.x), ih = tf32_rn(v.y);
-    p[i] = rh;
-    p[count + i] = tf32_rn(v.x - rh);
-    p[2 * count + i] = ih;
-    p[3 * count + i] = tf32_rn(v.y - ih);
+    float* o = pb + (row * (kpad / 8) + kk / 8) * 32 + (kk % 8);
+    o[0] = rh;
+    o[8] = tf32_rn(v.x - rh);
+    o[16] = ih;
+    o[24] = tf32_rn(v.y - ih);
   }
 }
 
@@ -351,17 +371,18 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 4-D map over planes laid out [batch][4][rows][k] (fp32), box
-// {BK, box_rows, 4, 1}, 32-byte swizzle.
-CUtensorMap plane_map(const float* base, std::uint64_t rows, std::uint64_t k, int batch, int box_rows) {
+// 4-D map over split planes laid out [batch][rows][kpad / 8][32] (fp32),
+// box {32, 1, box_rows, 1} (one 128-byte row per tile row), 128-byte swizzle.
+CUtensorMap plane_map(const float* base, std::uint64_t rows, std::uint64_t kpad, int batch, int box_rows) {
   CUtensorMap map;
   std::memset(&map, 0, sizeof(map));
-  const cuuint64_t dims[4] = {k, rows, 4, (cuuint64_t)batch};
-  const cuuint64_t strides[3] = {k * 4, rows * k * 4, 4 * rows * k * 4};
-  const cuuint32_t box[4] = {BK, (cuuint32_t)box_rows, 4, 1};
+  const std::uint64_t kb = kpad / 8;
+  const cuuint64_t dims[4] = {32, kb, rows, (cuuint64_t)batch};
+  const cuuint64_t strides[3] = {128, kb * 128, rows * kb * 128};
+  const cuuint32_t box[4] = {32, 1, (cuuint32_t)box_rows, 1};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(base), dims, strides,
-                           box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B,
+                           box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS)
     throw std::string("ERROR (qflex_gb300: tensor cores) --> cuTensorMapEncodeTiled failed: ") +
@@ -379,7 +400,9 @@ bool tc_eligible(std::size_t m, std::size_t n, std::size_t k) {
   return m >= 64 && n >= 64 && k >= 16 && k % 4 == 0 && m < (1u << 31) && n < (1u << 31) && k < (1u << 31);
 }
 
-std::size_t tc_workspace_elems(std::size_t m, std::size_t n, std::size_t k) { return 4 * (m + n) * k; }
+std::size_t tc_workspace_elems(std::size_t m, std::size_t n, std::size_t k) {
+  return 4 * (m + n) * ((k + 7) / 8 * 8);
+}
 
 void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size_t m, std::size_t n,
                          std::size_t k, std::uint64_t batch_stride, std::uint64_t bt_stride, int batch,
@@ -391,36 +414,35 @@ void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size
     // 8.7e-6 at 9.8, 4 -> max 1.6e-5 at 10.4. QFLEX_TC_CHUNK overrides 2.
     const char* e = std::getenv("QFLEX_TC_CHUNK");
     const int c = e ? std::atoi(e) : 2;
-    return (c == 1 || c == 4) ? c : 2;
+    return c >= 1 ? c : 2;
+  }();
+  // Epilogue warps poll the chunk barrier with this back-off (0: plain
+  // bounded wait); QFLEX_TC_EPI_SLEEP_NS overrides.
+  static const int epi_sleep = [] {
+    const char* e = std::getenv("QFLEX_TC_EPI_SLEEP_NS");
+    return e ? std::atoi(e) : 0;
   }();
   static std::once_flag attr;
   std::call_once(attr, [] {
-    check(cudaFuncSetAttribute(cgemm_tf32x3_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
-          "cudaFuncSetAttribute");
-    check(cudaFuncSetAttribute(cgemm_tf32x3_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
-          "cudaFuncSetAttribute");
-    check(cudaFuncSetAttribute(cgemm_tf32x3_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
+    check(cudaFuncSetAttribute(cgemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
           "cudaFuncSetAttribute");
   });
   float* pa = workspace;
-  float* pb = workspace + 4 * m * k * (std::size_t)batch;
+  const std::size_t kpad = (k + BK - 1) / BK * BK;
+  float* pb = workspace + 4 * m * kpad * (std::size_t)batch;
   {
     dim3 ga((unsigned)std::min<std::uint64_t>((m * k + 255) / 256, 152 * 16), (unsigned)batch);
-    split_tf32_kernel<<<ga, 256, 0, s>>>(A, pa, m * k, batch_stride);
+    split_tf32_kernel<<<ga, 256, 0, s>>>(A, pa, m, k, kpad, batch_stride);
     dim3 gb((unsigned)std::min<std::uint64_t>((n * k + 255) / 256, 152 * 16), (unsigned)batch);
-    split_tf32_kernel<<<gb, 256, 0, s>>>(Bt, pb, n * k, bt_stride);
+    split_tf32_kernel<<<gb, 256, 0, s>>>(Bt, pb, n, k, kpad, bt_stride);
     check(cudaGetLastError(), "split_tf32");
   }
-  const CUtensorMap ma = plane_map(pa, m, k, batch, BM);
-  const CUtensorMap mb = plane_map(pb, n, k, batch, BN);
+  const CUtensorMap ma = plane_map(pa, m, kpad, batch, BM);
+  const CUtensorMap mb = plane_map(pb, n, kpad, batch, BN);
   const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
   dim3 grid((unsigned)tiles, 1, (unsigned)batch);
-  if (chunk == 4)
-    cgemm_tf32x3_kernel<4><<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err);
-  else if (chunk == 2)
-    cgemm_tf32x3_kernel<2><<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err);
-  else
-    cgemm_tf32x3_kernel<1><<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err);
+  cgemm_tf32x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err,
+                                                        chunk, epi_sleep);
   check(cudaGetLastError(), "cgemm_tf32x3");
 }
 
