@@ -46,7 +46,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--batch", type=int, default=8, help="output strings per step")
     p.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    p.add_argument("--precision", default="fp32")
+    p.add_argument("--precision", default="tf32x3", choices=["tf32x3", "fp32"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
@@ -191,6 +191,35 @@ def dominant_kernel_time(ctx, torch, m, n, k, reps=5):
     return e0.elapsed_time(e1) / reps
 
 
+def accuracy_vs_fp64(ctx, circuit, ordering, grid, initial):
+    """Relative error of the amplitudes of the first output strings against
+    the committed FP64 oracle values (tests/golden/c3_fp64.json)."""
+    path = ROOT / "tests" / "golden" / "c3_fp64.json"
+    if not path.exists():
+        return None
+    ref = json.loads(path.read_text())
+    finals = [r["final"] for r in ref["amplitudes"]]
+    want = [complex(*r["amplitude"]) for r in ref["amplitudes"]]
+    got = [a for _, a in ctx.evaluate_many(circuit, ordering, grid, ref["initial"], finals, 1 << 40)]
+    errs = [abs(a - b) / abs(b) for a, b in zip(got, want)]
+    return {"max_rel_err_vs_fp64": max(errs), "per_amplitude": [float(f"{e:.3g}") for e in errs],
+            "amplitudes": len(errs), "reference": "FP64 oracle (complex128, double gate constants)"}
+
+
+def timed_steps(ctx, torch, stream, circuit, ordering, grid, initial, strings, first, steps):
+    """Runs `steps` evaluate_many calls; returns (device ms, event ms)."""
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    device_ms = 0.0
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for s in range(steps):
+        ctx.evaluate_many(circuit, ordering, grid, initial, strings(first + s), 1 << 40)
+        device_ms += ctx.stats()["device_ms"]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return device_ms, e0.elapsed_time(e1)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -208,10 +237,10 @@ def main():
         if world > 1:
             dist.barrier()
 
-    ctx = Context(local)
-    ctx.set_precision(args.precision)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
+    ctx = Context(local)
+    ctx.set_precision(args.precision)
     ctx.set_stream(stream.cuda_stream)
     circuit, ordering, grid, initial, finals = rqc.workload(WORKLOAD)
     B = args.batch
@@ -224,22 +253,12 @@ def main():
 
     for w in range(args.warmup):
         ctx.evaluate_many(circuit, ordering, grid, initial, strings(w), 1 << 40)
-    st = ctx.stats()
-    launches_per_step = int(st["n_ops"]) + 2
-
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    device_ms = 0.0
     with ClockSampler(local) as clocks:
         barrier()
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for s in range(args.steps):
-            ctx.evaluate_many(circuit, ordering, grid, initial, strings(args.warmup + s), 1 << 40)
-            device_ms += ctx.stats()["device_ms"]
-        e1.record(stream)
-        torch.cuda.synchronize()
+        device_ms, e2e_ms = timed_steps(ctx, torch, stream, circuit, ordering, grid, initial, strings,
+                                        args.warmup, args.steps)
         barrier()
-    e2e_ms = e0.elapsed_time(e1)
+    st = ctx.stats()
     if world > 1:
         t = torch.tensor([device_ms, e2e_ms], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -248,32 +267,66 @@ def main():
     value = amps / (device_ms / 1000.0)
     e2e = amps / (e2e_ms / 1000.0)
 
-    # Roofline of the dominant kernel (the 4096^3 complex product).
-    shapes = sorted(ctx.shapes(), key=lambda x: -x[0] * x[1] * x[2] * x[3])
-    m, n, k, _ = shapes[0]
-    kt_ms = dominant_kernel_time(ctx, torch, m, n, k)
-    achieved = 8.0 * m * n * k / (kt_ms / 1e3) / 1e12
-    roofline = {"bound": "fp32", "kernel": f"cgemm_fp32 ({m},{n},{k})", "achieved": achieved,
-                "peak": FP32_PEAK_NOMINAL, "unit": "TFLOP/s", "frac": achieved / FP32_PEAK_NOMINAL,
-                "peak_source": "nominal FP32 CUDA-core FMA rate (152 SMs x 128 lanes x 2 x 2.07 GHz); "
-                               "MEASURED_PEAKS.json has no FP32 CUDA-core figure",
-                "traffic": None, "timing": "CUDA events on the context stream, dominant shape, 5 launches"}
-    gflop = st["gemm_flop"]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": e2e_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
             "config": config(args),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * 49 * B,
                     "d2h_bytes_per_step": 16 * B},
-            "gpu_launches": launches_per_step * args.steps,
-            "algorithmic_tflops": gflop * B * args.steps * world / (device_ms / 1e3) / 1e12,
-            "roofline": roofline, "clocks": clocks.summary(),
-            "plan": {"gemm_flop_per_amplitude": gflop, "permute_bytes_per_amplitude": st["permute_bytes"],
+            "gpu_launches": int(st["launches"]) * args.steps,
+            "algorithmic_tflops": st["gemm_flop"] * amps / (device_ms / 1e3) / 1e12,
+            "clocks": clocks.summary(),
+            "plan": {"gemm_flop_per_amplitude": st["gemm_flop"],
+                     "permute_bytes_per_amplitude": st["permute_bytes"],
                      "arena_bytes_per_string": st["arena_bytes"], "ops": st["n_ops"],
                      "slices": st["n_leaves"]}}
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        dt, v, desc, cores = cpu_sample()
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+
+    if rank == 0 and world == 1:
+        # Accuracy of this path, then the plain FP32 CUDA-core path timed on
+        # the same workload for the ratio the metric asks for.
+        line["accuracy"] = accuracy_vs_fp64(ctx, circuit, ordering, grid, initial)
+        shapes = sorted(ctx.shapes(), key=lambda x: -x[0] * x[1] * x[2] * x[3])
+        m, n, k, _ = shapes[0]
+        kt_ms = dominant_kernel_time(ctx, torch, m, n, k)
+        achieved = 8.0 * m * n * k / (kt_ms / 1e3) / 1e12
+        pk = peaks()
+        if args.precision == "fp32":
+            line["roofline"] = {
+                "bound": "fp32", "kernel": f"cgemm_fp32 ({m},{n},{k})", "achieved": achieved,
+                "peak": FP32_PEAK_NOMINAL, "unit": "TFLOP/s", "frac": achieved / FP32_PEAK_NOMINAL,
+                "peak_source": "nominal FP32 CUDA-core FMA rate (152 SMs x 128 lanes x 2 x 2.07 GHz); "
+                               "the measured peaks hold no FP32 CUDA-core figure",
+                "traffic": None, "timing": "CUDA events, dominant shape, 5 launches"}
+        else:
+            # 3xTF32 with 4 real products = 12 TF32 MMAs of 2mnk per 8mnk of
+            # algorithmic work; the TF32 dense rate is half the bf16 rate.
+            bf16 = pk.get("bf16_tflops", 1900.0)
+            tf32_peak = bf16 / 2
+            line["roofline"] = {
+                "bound": "tensor", "kernel": f"cgemm_tf32x3 ({m},{n},{k}) incl. plane splits",
+                "achieved": 3.0 * achieved, "achieved_algorithmic": achieved, "peak": tf32_peak,
+                "unit": "TFLOP/s (TF32 MMA)", "frac": 3.0 * achieved / tf32_peak,
+                "peak_source": ("measured bf16 dense burst / 2 (MEASURED_PEAKS.json)" if "bf16_tflops" in pk
+                                else "fallback 1.9 PFLOP/s bf16 / 2"),
+                "traffic": 2.322e9 if (m, n, k) == (4096, 4096, 4096) else None,
+                "traffic_source": "ncu dram__bytes_read+write of one (4096,4096,4096) launch, "
+                                  "profiles/tc_gemm_4096.md",
+                "timing": "CUDA events on the context stream, dominant shape, 5 launches"}
+            fp = Context(local)
+            fp.set_precision("fp32")
+            fp.set_stream(stream.cuda_stream)
+            fp.evaluate_many(circuit, ordering, grid, initial, strings(0), 1 << 40)
+            f_dev, _ = timed_steps(fp, torch, stream, circuit, ordering, grid, initial, strings,
+                                   args.warmup, 1)
+            fp32_value = B / (f_dev / 1000.0)
+            line["fp32_path"] = {"value": fp32_value, "unit": UNIT, "steps": 1,
+                                 "speedup_of_this_path": value / fp32_value,
+                                 "accuracy": accuracy_vs_fp64(fp, circuit, ordering, grid, initial)}
+            fp.close()
+        if not args.no_cpu_baseline:
+            dt, v, desc, cores = cpu_sample()
+            line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                    "sample": desc}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -44,6 +44,7 @@ typedef struct {
   size_t n_ops;           /* device ops of the program */
   size_t n_leaves;        /* contraction leaves (cut slices x terminal values) */
   size_t batch;           /* final states evaluated per device pass */
+  size_t launches;        /* kernel launches of the last evaluation */
 } qflex_gb300_stats;
 
 /* Creates a context on CUDA device `device`. No reference counterpart (the

@@ -47,6 +47,7 @@ class Stats(C.Structure):
         ("n_ops", C.c_size_t),
         ("n_leaves", C.c_size_t),
         ("batch", C.c_size_t),
+        ("launches", C.c_size_t),
     ]
 
     def as_dict(self) -> dict:

@@ -181,6 +181,7 @@ int qflex_gb300_last_stats(const qflex_gb300_context* ctx, qflex_gb300_stats* ou
   out->n_ops = s.n_ops;
   out->n_leaves = s.n_leaves;
   out->batch = s.batch;
+  out->launches = s.launches;
   return QFLEX_GB300_OK;
 }
 

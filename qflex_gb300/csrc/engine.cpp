@@ -251,8 +251,9 @@ T* upload(const std::vector<T>& v) {
 
 }  // namespace
 
-void Engine::run_program(Plan& p, int batch, float2* arena, float* tc_ws) {
+std::size_t Engine::run_program(Plan& p, int batch, float2* arena, float* tc_ws) {
   const Program& prog = p.prog;
+  std::size_t launches = 0;
   const std::uint64_t stride = prog.arena_elems;
   float2* scratch = skinny_scratch();
   int* err = error_flag();
@@ -260,14 +261,18 @@ void Engine::run_program(Plan& p, int batch, float2* arena, float* tc_ws) {
     const DevOp& op = prog.ops[i];
     if (op.kind == DevOp::PERMUTE) {
       launch_permute(p.perm[i], arena + op.a, arena + op.c, stride, batch, stream_);
+      launches += 1;
     } else if (op.b_nk) {
       launch_cgemm_tf32x3(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, stride,
                           batch, tc_ws, err, stream_);
+      launches += 3;  // two plane splits and the product
     } else {
       launch_cgemm_fp32(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, batch,
                         stream_, scratch);
+      launches += skinny_splits(op.m, op.n, op.k, batch) ? 2 : 1;
     }
   }
+  return launches;
 }
 
 float2* Engine::skinny_scratch() {
@@ -402,6 +407,7 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
   }
   std::vector<double2> h_amps(std::max<std::size_t>(n_amps, 1) * (std::size_t)chunk);
   double ms_total = 0;
+  std::size_t launches = 0;
   for (int f0 = 0; f0 < total; f0 += chunk) {
     const int nb = std::min(chunk, total - f0);
     bits.assign(n_cols * 2 * (std::size_t)nb, 0);
@@ -417,7 +423,7 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
     QFX_CUDA(cudaEventRecord(ev0_, stream_));
     launch_flatten(p.d_cols, (int)n_cols, p.max_size_log2, p.d_steps, p.d_mats, p.d_mats_lo, d_bits,
                    d_bits + n_cols * (std::size_t)nb, arena, prog.arena_elems, nb, stream_);
-    run_program(p, nb, arena, tc_ws);
+    launches += run_program(p, nb, arena, tc_ws) + 2;  // + flatten and sums
     launch_reduce_amplitudes(arena + prog.results_offset, prog.arena_elems, p.d_ptr, p.d_leaves,
                              (int)n_amps, d_amps, nb, stream_);
     QFX_CUDA(cudaEventRecord(ev1_, stream_));
@@ -438,6 +444,7 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
   }
   if (p.tc_ws_elems) check_error_flag();
   stats_.device_ms = ms_total;
+  stats_.launches = launches;
   stats_.batch = (std::size_t)chunk;
   return results;
 }

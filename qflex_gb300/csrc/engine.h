@@ -31,6 +31,7 @@ struct RunStats {
   std::size_t n_ops = 0;
   std::size_t n_leaves = 0;
   std::size_t batch = 0;
+  std::size_t launches = 0;   // kernel launches of the last evaluation
   double reference_bytes = 0;
 };
 
@@ -78,7 +79,7 @@ class Engine {
  private:
   struct Plan;
   Plan* get_plan(const std::string& circuit, const std::string& ordering, const std::string& grid);
-  void run_program(Plan& p, int batch, float2* arena, float* tc_ws);
+  std::size_t run_program(Plan& p, int batch, float2* arena, float* tc_ws);
 
   int device_;
   int precision_;
