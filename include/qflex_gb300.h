@@ -104,6 +104,17 @@ size_t qflex_gb300_last_shapes(const qflex_gb300_context* ctx, size_t* out, size
  * same order. Returns the number of products. */
 size_t qflex_gb300_last_gemms(const qflex_gb300_context* ctx, size_t* out, size_t cap);
 
+/* Per-op timing, the engine's counterpart of the reference's verbose
+ * per-multiply timings ("[R] reordering", "[M] multiplying",
+ * src/tensor.cpp:1059-1193). With profiling on, every device op of an
+ * evaluation is bracketed by CUDA events (captured graphs are not used).
+ * qflex_gb300_last_ops writes up to `cap` rows of 8 doubles per op of the
+ * last plan -- kind (0 permute, 1 CUDA-core product, 2 tensor-core product,
+ * 3 split-k skinny product), m, n, k (permute: m = elements), flop, bytes,
+ * batch, milliseconds (-1 if not profiled) -- and returns the op count. */
+int qflex_gb300_set_profiling(qflex_gb300_context* ctx, int on);
+size_t qflex_gb300_last_ops(const qflex_gb300_context* ctx, double* out, size_t cap);
+
 /* ---- tensor-level operations on device memory (complex64, interleaved) ----
  * Pointers are CUDA device pointers; work is queued on the context's stream.
  */
@@ -138,6 +149,26 @@ int qflex_gb300_multiply(qflex_gb300_context* ctx, const void* A, const void* B,
                          size_t n, size_t k, size_t batch, size_t batch_stride);
 
 int qflex_gb300_synchronize(qflex_gb300_context* ctx);
+
+/* ---- learned cost model kernels ----
+ * A 3-layer perceptron y = W3 relu(W2 relu(W1 x + b1) + b2) + b3 in FP32
+ * that predicts an op's log time from its features; it ranks candidate
+ * orderings the way the reference's auto-orderer ranks them with its
+ * analytic cost (qflexcirq/ordering/order_circuit_simulation.py:87-106).
+ * No counterpart in the reference's C++ core. All pointers are device
+ * pointers; work is queued on `stream`. `work` holds
+ * qflex_gb300_mlp_work_floats(n, hidden) floats. */
+size_t qflex_gb300_mlp_param_count(int d_in, int hidden);
+size_t qflex_gb300_mlp_work_floats(size_t n, int hidden);
+int qflex_gb300_mlp_forward(void* stream, const float* params, const float* X, size_t n, int d_in, int hidden,
+                            float* work, float* y);
+/* Mean-squared error against `target` (written to *loss, device) and its
+ * gradient with respect to every parameter (written to `grads`). */
+int qflex_gb300_mlp_loss_grad(void* stream, const float* params, const float* X, const float* target, size_t n,
+                              int d_in, int hidden, float* work, float* grads, float* loss);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8); `step` counts from 1. */
+int qflex_gb300_mlp_adam(void* stream, float* params, const float* grads, float* m, float* v, size_t count,
+                         int step, float lr);
 
 /* Skinny product that allocates no device memory: C[m,n] = A[m,k] * B[k,n]
  * (row-major complex64) for at most 64 outputs (m * n <= 64, m, n <= 64),

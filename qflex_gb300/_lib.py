@@ -23,9 +23,12 @@ EXPORTS = (
     "qflex_gb300_evaluate_many", "qflex_gb300_result_count", "qflex_gb300_result_state",
     "qflex_gb300_result_amplitude", "qflex_gb300_result_initial_state",
     "qflex_gb300_result_final_state", "qflex_gb300_last_stats", "qflex_gb300_last_shapes",
-    "qflex_gb300_last_gemms", "qflex_gb300_permute", "qflex_gb300_check_permute",
+    "qflex_gb300_last_gemms", "qflex_gb300_set_profiling", "qflex_gb300_last_ops",
+    "qflex_gb300_permute", "qflex_gb300_check_permute",
     "qflex_gb300_reorder",
-    "qflex_gb300_multiply", "qflex_gb300_synchronize", "qflex_gb300_multiply_skinny_noalloc",
+    "qflex_gb300_multiply", "qflex_gb300_synchronize", "qflex_gb300_mlp_param_count",
+    "qflex_gb300_mlp_work_floats", "qflex_gb300_mlp_forward", "qflex_gb300_mlp_loss_grad",
+    "qflex_gb300_mlp_adam", "qflex_gb300_multiply_skinny_noalloc",
 )
 
 
@@ -86,12 +89,19 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
             "qflex_gb300_last_stats": (i, [vp, C.POINTER(Stats)]),
             "qflex_gb300_last_shapes": (sz, [vp, C.POINTER(sz), sz]),
             "qflex_gb300_last_gemms": (sz, [vp, C.POINTER(sz), sz]),
+            "qflex_gb300_set_profiling": (i, [vp, i]),
+            "qflex_gb300_last_ops": (sz, [vp, C.POINTER(dbl), sz]),
             "qflex_gb300_permute": (i, [vp, vp, vp, sz, C.POINTER(sz), C.POINTER(sz), sz, sz]),
             "qflex_gb300_check_permute": (i, [sz, C.POINTER(sz), C.POINTER(sz), vp, vp]),
             "qflex_gb300_reorder": (i, [vp, vp, vp, sz, C.POINTER(sz), C.POINTER(sz)]),
             "qflex_gb300_multiply": (i, [vp, vp, vp, vp, sz, sz, sz, sz, sz]),
             "qflex_gb300_synchronize": (i, [vp]),
             "qflex_gb300_multiply_skinny_noalloc": (i, [vp, vp, vp, sz, sz, sz, vp, C.c_char_p, sz]),
+            "qflex_gb300_mlp_param_count": (sz, [i, i]),
+            "qflex_gb300_mlp_work_floats": (sz, [sz, i]),
+            "qflex_gb300_mlp_forward": (i, [vp, vp, vp, sz, i, i, vp, vp]),
+            "qflex_gb300_mlp_loss_grad": (i, [vp, vp, vp, vp, sz, i, i, vp, vp, vp]),
+            "qflex_gb300_mlp_adam": (i, [vp, vp, vp, vp, vp, sz, i, C.c_float]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -224,6 +234,18 @@ class Context:
         buf = (C.c_size_t * (3 * max(n, 1)))()
         self._lib.qflex_gb300_last_gemms(self._h, buf, n)
         return [tuple(buf[3 * i:3 * i + 3]) for i in range(n)]
+
+    def set_profiling(self, on: bool) -> None:
+        self._check(self._lib.qflex_gb300_set_profiling(self._h, 1 if on else 0))
+
+    def ops(self):
+        """Device ops of the last plan as a (n_ops, 8) numpy array: kind, m,
+        n, k, flop, bytes, batch, milliseconds (-1 unless profiled)."""
+        import numpy as np
+        n = self._lib.qflex_gb300_last_ops(self._h, None, 0)
+        buf = (C.c_double * (8 * max(n, 1)))()
+        self._lib.qflex_gb300_last_ops(self._h, buf, n)
+        return np.frombuffer(buf, dtype=np.float64)[:8 * n].reshape(n, 8).copy()
 
     # ---- tensor-level device operations (pointers are CUDA addresses) ----
     def permute(self, src: int, dst: int, dims: Sequence[int], new_order: Sequence[int],

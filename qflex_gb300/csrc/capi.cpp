@@ -212,6 +212,24 @@ size_t qflex_gb300_last_gemms(const qflex_gb300_context* ctx, size_t* out, size_
   return n;
 }
 
+int qflex_gb300_set_profiling(qflex_gb300_context* ctx, int on) {
+  return guarded(ctx, [&] {
+    if (!ctx->engine) throw QFX_ERR("context has no engine");
+    ctx->engine->set_profiling(on != 0);
+  });
+}
+
+size_t qflex_gb300_last_ops(const qflex_gb300_context* ctx, double* out, size_t cap) {
+  if (!ctx || !ctx->engine) return 0;
+  const auto ops = ctx->engine->last_ops();
+  for (size_t i = 0; i < ops.size() && i < cap && out; ++i) {
+    const auto& r = ops[i];
+    const double row[8] = {double(r.kind), r.m, r.n, r.k, r.flop, r.bytes, r.batch, r.ms};
+    std::memcpy(out + 8 * i, row, sizeof(row));
+  }
+  return ops.size();
+}
+
 int qflex_gb300_permute(qflex_gb300_context* ctx, const void* src, void* dst, size_t rank,
                         const size_t* dims, const size_t* new_order, size_t batch,
                         size_t batch_stride) {

@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <unordered_map>
 
@@ -21,6 +22,18 @@ std::string cuda_error_string(cudaError_t e, const char* what) {
     cudaError_t e_ = (call);                                            \
     if (e_ != cudaSuccess) throw cuda_error_string(e_, #call);          \
   } while (0)
+
+// Identifies the buffers a captured device pass was recorded with.
+struct GraphKey {
+  int batch = 0;
+  const void* arena = nullptr;
+  const void* ws = nullptr;
+  const void* bits = nullptr;
+  const void* amps = nullptr;
+  bool operator==(const GraphKey& o) const {
+    return batch == o.batch && arena == o.arena && ws == o.ws && bits == o.bits && amps == o.amps;
+  }
+};
 
 struct Engine::Plan {
   std::string key;
@@ -41,7 +54,12 @@ struct Engine::Plan {
   float2* d_mats_lo = nullptr;  // null: plain FP32 columns
   std::uint32_t* d_ptr = nullptr;
   std::uint32_t* d_leaves = nullptr;
+  // Captured device pass and the buffers it was captured with.
+  cudaGraphExec_t graph = nullptr;
+  GraphKey graph_key, seen_key;
+  std::size_t graph_launches = 0;
   ~Plan() {
+    if (graph) cudaGraphExecDestroy(graph);
     cudaFree(d_cols);
     cudaFree(d_steps);
     cudaFree(d_mats);
@@ -62,6 +80,7 @@ Engine::Engine(int device, int precision) : device_(device), precision_(precisio
   QFX_CUDA(cudaSetDevice(device_));
   QFX_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
   own_stream_ = true;
+  if (const char* g = std::getenv("QFLEX_GB300_GRAPHS")) graphs_ = std::atoi(g) != 0;
   QFX_CUDA(cudaEventCreate(&ev0_));
   QFX_CUDA(cudaEventCreate(&ev1_));
   set_precision(precision);
@@ -75,6 +94,7 @@ Engine::~Engine() {
   for (auto& b : bufs_) cudaFree(b.ptr);
   if (ev0_) cudaEventDestroy(ev0_);
   if (ev1_) cudaEventDestroy(ev1_);
+  for (auto e : prof_events_) cudaEventDestroy(e);
   if (own_stream_ && stream_) cudaStreamDestroy(stream_);
 }
 
@@ -257,8 +277,16 @@ std::size_t Engine::run_program(Plan& p, int batch, float2* arena, float* tc_ws)
   const std::uint64_t stride = prog.arena_elems;
   float2* scratch = skinny_scratch();
   int* err = error_flag();
+  if (profile_) {
+    while (prof_events_.size() < prog.ops.size() + 1) {
+      cudaEvent_t e;
+      QFX_CUDA(cudaEventCreate(&e));
+      prof_events_.push_back(e);
+    }
+  }
   for (std::size_t i = 0; i < prog.ops.size(); ++i) {
     const DevOp& op = prog.ops[i];
+    if (profile_) QFX_CUDA(cudaEventRecord(prof_events_[i], stream_));
     if (op.kind == DevOp::PERMUTE) {
       launch_permute(p.perm[i], arena + op.a, arena + op.c, stride, batch, stream_);
       launches += 1;
@@ -272,7 +300,35 @@ std::size_t Engine::run_program(Plan& p, int batch, float2* arena, float* tc_ws)
       launches += skinny_splits(op.m, op.n, op.k, batch) ? 2 : 1;
     }
   }
+  if (profile_) QFX_CUDA(cudaEventRecord(prof_events_[prog.ops.size()], stream_));
   return launches;
+}
+
+std::vector<OpRecord> Engine::last_ops() const {
+  std::vector<OpRecord> out;
+  if (!plan_ || !plan_->built) return out;
+  const Program& prog = plan_->prog;
+  for (std::size_t i = 0; i < prog.ops.size(); ++i) {
+    const DevOp& op = prog.ops[i];
+    OpRecord r{};
+    if (op.kind == DevOp::PERMUTE) {
+      r.kind = 0;
+      r.m = double(std::size_t(1) << op.nbits);
+      r.n = r.k = 1;
+      r.bytes = 16.0 * r.m;
+    } else {
+      r.kind = op.b_nk ? 2 : (skinny_splits(op.m, op.n, op.k, (int)std::max<std::size_t>(stats_.batch, 1)) ? 3 : 1);
+      r.m = double(op.m);
+      r.n = double(op.n);
+      r.k = double(op.k);
+      r.flop = 8.0 * r.m * r.n * r.k;
+      r.bytes = 8.0 * (r.m * r.k + r.k * r.n + r.m * r.n);
+    }
+    r.batch = double(std::max<std::size_t>(stats_.batch, 1));
+    r.ms = i < op_ms_.size() ? op_ms_[i] : -1.0;
+    out.push_back(r);
+  }
+  return out;
 }
 
 float2* Engine::skinny_scratch() {
@@ -421,11 +477,46 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
     QFX_CUDA(cudaMemcpyAsync(d_bits, bits.data(), bits.size(), cudaMemcpyHostToDevice, stream_));
     QFX_CUDA(cudaMemsetAsync(d_amps, 0, std::max<std::size_t>(n_amps, 1) * sizeof(double2) * nb, stream_));
     QFX_CUDA(cudaEventRecord(ev0_, stream_));
-    launch_flatten(p.d_cols, (int)n_cols, p.max_size_log2, p.d_steps, p.d_mats, p.d_mats_lo, d_bits,
-                   d_bits + n_cols * (std::size_t)nb, arena, prog.arena_elems, nb, stream_);
-    launches += run_program(p, nb, arena, tc_ws) + 2;  // + flatten and sums
-    launch_reduce_amplitudes(arena + prog.results_offset, prog.arena_elems, p.d_ptr, p.d_leaves,
-                             (int)n_amps, d_amps, nb, stream_);
+    auto enqueue = [&]() -> std::size_t {
+      launch_flatten(p.d_cols, (int)n_cols, p.max_size_log2, p.d_steps, p.d_mats, p.d_mats_lo, d_bits,
+                     d_bits + n_cols * (std::size_t)nb, arena, prog.arena_elems, nb, stream_);
+      const std::size_t l = run_program(p, nb, arena, tc_ws) + 2;  // + flatten and sums
+      launch_reduce_amplitudes(arena + prog.results_offset, prog.arena_elems, p.d_ptr, p.d_leaves,
+                               (int)n_amps, d_amps, nb, stream_);
+      return l;
+    };
+    // The whole pass (flatten, program, sums) is one CUDA graph once the
+    // same batch size and buffers repeat: the first pass runs eagerly, the
+    // second is captured, later ones replay the graph.
+    const GraphKey gk{nb, arena, tc_ws, d_bits, d_amps};
+    if (!profile_ && p.graph && p.graph_key == gk) {
+      QFX_CUDA(cudaGraphLaunch(p.graph, stream_));
+      launches += p.graph_launches;
+    } else if (!profile_ && graphs_ && p.seen_key == gk) {
+      if (p.graph) cudaGraphExecDestroy(p.graph);
+      p.graph = nullptr;
+      cudaGraph_t g = nullptr;
+      QFX_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+      std::size_t l = 0;
+      try {
+        l = enqueue();
+      } catch (...) {
+        cudaStreamEndCapture(stream_, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      QFX_CUDA(cudaStreamEndCapture(stream_, &g));
+      const cudaError_t ie = cudaGraphInstantiate(&p.graph, g, 0);
+      cudaGraphDestroy(g);
+      if (ie != cudaSuccess) throw cuda_error_string(ie, "cudaGraphInstantiate");
+      p.graph_key = gk;
+      p.graph_launches = l;
+      QFX_CUDA(cudaGraphLaunch(p.graph, stream_));
+      launches += l;
+    } else {
+      launches += enqueue();
+      p.seen_key = gk;
+    }
     QFX_CUDA(cudaEventRecord(ev1_, stream_));
     QFX_CUDA(cudaMemcpyAsync(h_amps.data(), d_amps, n_amps * sizeof(double2) * nb,
                              cudaMemcpyDeviceToHost, stream_));
@@ -433,6 +524,14 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
     float ms = 0;
     QFX_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
     ms_total += ms;
+    if (profile_) {
+      op_ms_.assign(prog.ops.size(), 0.0);
+      for (std::size_t i = 0; i < prog.ops.size(); ++i) {
+        float t = 0;
+        QFX_CUDA(cudaEventElapsedTime(&t, prof_events_[i], prof_events_[i + 1]));
+        op_ms_[i] = t;
+      }
+    }
     for (int b = 0; b < nb; ++b) {
       auto& r = results[f0 + b];
       r.amplitudes.resize(n_amps);

@@ -35,6 +35,16 @@ struct RunStats {
   double reference_bytes = 0;
 };
 
+// One device op of the last plan with its measured time (profiling on).
+struct OpRecord {
+  int kind;        // 0 permute, 1 CUDA-core product, 2 tensor-core product, 3 split-k skinny product
+  double m, n, k;  // product shape (permute: m = elements)
+  double flop;     // 8 m n k
+  double bytes;    // operand + result bytes (permute: read + write)
+  double batch;    // final states per device pass
+  double ms;       // CUDA-event time of the op, -1 when not profiled
+};
+
 class Engine {
  public:
   Engine(int device, int precision);
@@ -60,6 +70,10 @@ class Engine {
   const std::vector<GemmShape>& last_shapes() const;
   // The last planned program (null before the first evaluation).
   const Program* last_program() const;
+  // Per-op timing: with profiling on, every device op is bracketed by CUDA
+  // events (graph replay is off) and last_ops() reports each op's time.
+  void set_profiling(bool on) { profile_ = on; }
+  std::vector<OpRecord> last_ops() const;
 
   // Device buffers owned by the engine, reused across calls.
   void* reserve(std::size_t bytes, int slot);
@@ -85,6 +99,10 @@ class Engine {
   int precision_;
   cudaStream_t stream_ = nullptr;
   bool own_stream_ = false;
+  bool graphs_ = true;  // capture repeated device passes (QFLEX_GB300_GRAPHS=0 disables)
+  bool profile_ = false;
+  std::vector<cudaEvent_t> prof_events_;
+  std::vector<double> op_ms_;
   std::unique_ptr<Plan> plan_;
   struct DevBuf {
     void* ptr = nullptr;
