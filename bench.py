@@ -48,6 +48,8 @@ def parse():
     p.add_argument("--impl", default="engine", choices=["engine", "reference"])
     p.add_argument("--precision", default="tf32x3", choices=["tf32x3", "fp32"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="skip the tensor-core kernel / strings-per-pass autotuning before warm-up")
     return p.parse_args()
 
 
@@ -251,6 +253,13 @@ def main():
         base = ((step * world) + rank) * B
         return [finals[(base + i) % len(finals)] for i in range(B)]
 
+    tuned = None
+    if args.precision == "tf32x3" and not args.no_autotune:
+        # Untimed: kernel variant per product shape, strings per device pass
+        # (on strings from the end of the list, not used by the steps).
+        from qflex_gb300 import autotune
+        tuned = autotune.tune(ctx, circuit, ordering, grid, initial, finals[-B:],
+                              batches=[b for b in (1, 2, 4, 8, 16) if b <= B], stream=stream)
     for w in range(args.warmup):
         ctx.evaluate_many(circuit, ordering, grid, initial, strings(w), 1 << 40)
     with ClockSampler(local) as clocks:
@@ -270,7 +279,9 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": e2e_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-            "config": config(args),
+            "config": dict(config(args), autotune=None if tuned is None else {
+                "variants": {sh: r["variant"] for sh, r in tuned["products"].items()},
+                "max_batch": tuned["max_batch"]}),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * 49 * B,
                     "d2h_bytes_per_step": 16 * B},
             "gpu_launches": int(st["launches"]) * args.steps,

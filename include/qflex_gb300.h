@@ -115,6 +115,27 @@ size_t qflex_gb300_last_gemms(const qflex_gb300_context* ctx, size_t* out, size_
 int qflex_gb300_set_profiling(qflex_gb300_context* ctx, int on);
 size_t qflex_gb300_last_ops(const qflex_gb300_context* ctx, double* out, size_t cap);
 
+/* Tuning options of a context; no reference counterpart (the reference has
+ * no device kernels to tune). Names and values:
+ *   "tc_chunk"   k-steps of 8 per TMEM accumulation chunk of the split
+ *                tensor-core product, 1..64 (default 2, or QFLEX_TC_CHUNK;
+ *                longer chunks are faster and less accurate: the tensor
+ *                core's FP32 accumulation truncates)
+ *   "tc_pair"    1: products with m >= 256 use the CTA-pair (cta_group::2,
+ *                256 x 128 tile) kernel; 0: every product uses the
+ *                single-CTA 128 x 128 tile (default 1, or QFLEX_TC_PAIR)
+ *   "graphs"     1: capture a repeated device pass in a CUDA graph and
+ *                replay it (default 1, or QFLEX_GB300_GRAPHS)
+ *   "max_batch"  most output strings per device pass of evaluate_many
+ *                (0: as many as fit in device memory; default 0)
+ * Unknown names and out-of-range values return QFLEX_GB300_ERR_ARG. */
+int qflex_gb300_set_option(qflex_gb300_context* ctx, const char* name, double value);
+int qflex_gb300_get_option(const qflex_gb300_context* ctx, const char* name, double* value);
+/* Tensor-core kernel for products of shape (m, n, k), e.g. chosen by an
+ * autotuner: 0 single CTA, 1 CTA pair (needs m >= 64), -1 removes the
+ * override. Overrides "tc_pair" for that shape. */
+int qflex_gb300_set_tc_variant(qflex_gb300_context* ctx, size_t m, size_t n, size_t k, int variant);
+
 /* ---- tensor-level operations on device memory (complex64, interleaved) ----
  * Pointers are CUDA device pointers; work is queued on the context's stream.
  */

@@ -24,6 +24,7 @@ EXPORTS = (
     "qflex_gb300_result_amplitude", "qflex_gb300_result_initial_state",
     "qflex_gb300_result_final_state", "qflex_gb300_last_stats", "qflex_gb300_last_shapes",
     "qflex_gb300_last_gemms", "qflex_gb300_set_profiling", "qflex_gb300_last_ops",
+    "qflex_gb300_set_option", "qflex_gb300_get_option", "qflex_gb300_set_tc_variant",
     "qflex_gb300_permute", "qflex_gb300_check_permute",
     "qflex_gb300_reorder",
     "qflex_gb300_multiply", "qflex_gb300_synchronize", "qflex_gb300_mlp_param_count",
@@ -90,6 +91,9 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
             "qflex_gb300_last_shapes": (sz, [vp, C.POINTER(sz), sz]),
             "qflex_gb300_last_gemms": (sz, [vp, C.POINTER(sz), sz]),
             "qflex_gb300_set_profiling": (i, [vp, i]),
+            "qflex_gb300_set_option": (i, [vp, C.c_char_p, dbl]),
+            "qflex_gb300_get_option": (i, [vp, C.c_char_p, C.POINTER(dbl)]),
+            "qflex_gb300_set_tc_variant": (i, [vp, sz, sz, sz, i]),
             "qflex_gb300_last_ops": (sz, [vp, C.POINTER(dbl), sz]),
             "qflex_gb300_permute": (i, [vp, vp, vp, sz, C.POINTER(sz), C.POINTER(sz), sz, sz]),
             "qflex_gb300_check_permute": (i, [sz, C.POINTER(sz), C.POINTER(sz), vp, vp]),
@@ -237,6 +241,22 @@ class Context:
 
     def set_profiling(self, on: bool) -> None:
         self._check(self._lib.qflex_gb300_set_profiling(self._h, 1 if on else 0))
+
+    def set_option(self, name: str, value: float) -> None:
+        """Tuning option: tc_chunk, tc_pair, graphs or max_batch."""
+        self._check(self._lib.qflex_gb300_set_option(self._h, name.encode(), float(value)))
+
+    def get_option(self, name: str) -> float:
+        v = C.c_double()
+        rc = self._lib.qflex_gb300_get_option(self._h, name.encode(), C.byref(v))
+        if rc != 0:
+            raise QflexGb300Error(rc, f"unknown option {name!r}")
+        return v.value
+
+    def set_tc_variant(self, m: int, n: int, k: int, variant: int) -> None:
+        """Tensor-core kernel for products of shape (m, n, k): 0 single CTA,
+        1 CTA pair, -1 no override."""
+        self._check(self._lib.qflex_gb300_set_tc_variant(self._h, m, n, k, int(variant)))
 
     def ops(self):
         """Device ops of the last plan as a (n_ops, 8) numpy array: kind, m,

@@ -212,6 +212,33 @@ size_t qflex_gb300_last_gemms(const qflex_gb300_context* ctx, size_t* out, size_
   return n;
 }
 
+int qflex_gb300_set_option(qflex_gb300_context* ctx, const char* name, double value) {
+  if (!name) return QFLEX_GB300_ERR_ARG;
+  int rc = guarded(ctx, [&] {
+    if (!ctx->engine) throw QFX_ERR("context has no engine");
+    ctx->engine->set_option(name, value);
+  });
+  return rc == QFLEX_GB300_ERR_INPUT ? QFLEX_GB300_ERR_ARG : rc;
+}
+
+int qflex_gb300_get_option(const qflex_gb300_context* ctx, const char* name, double* value) {
+  if (!ctx || !ctx->engine || !name || !value) return QFLEX_GB300_ERR_ARG;
+  try {
+    *value = ctx->engine->get_option(name);
+  } catch (...) {
+    return QFLEX_GB300_ERR_ARG;
+  }
+  return QFLEX_GB300_OK;
+}
+
+int qflex_gb300_set_tc_variant(qflex_gb300_context* ctx, size_t m, size_t n, size_t k, int variant) {
+  int rc = guarded(ctx, [&] {
+    if (!ctx->engine) throw QFX_ERR("context has no engine");
+    ctx->engine->set_tc_variant(m, n, k, variant);
+  });
+  return rc == QFLEX_GB300_ERR_INPUT ? QFLEX_GB300_ERR_ARG : rc;
+}
+
 int qflex_gb300_set_profiling(qflex_gb300_context* ctx, int on) {
   return guarded(ctx, [&] {
     if (!ctx->engine) throw QFX_ERR("context has no engine");

@@ -30,8 +30,11 @@ struct GraphKey {
   const void* ws = nullptr;
   const void* bits = nullptr;
   const void* amps = nullptr;
+  unsigned options = 0;
+  int precision = -1;
   bool operator==(const GraphKey& o) const {
-    return batch == o.batch && arena == o.arena && ws == o.ws && bits == o.bits && amps == o.amps;
+    return batch == o.batch && arena == o.arena && ws == o.ws && bits == o.bits && amps == o.amps &&
+           options == o.options && precision == o.precision;
   }
 };
 
@@ -69,7 +72,7 @@ struct Engine::Plan {
   }
 };
 
-Engine::Engine(int device, int precision) : device_(device), precision_(precision) {
+Engine::Engine(int device, int precision) : device_(device), precision_(precision), tc_cfg_(tc_default_config()) {
   if (device < 0) {  // planning only: no CUDA calls at all
     set_precision(precision);
     return;
@@ -101,6 +104,51 @@ Engine::~Engine() {
 void Engine::set_precision(int p) {
   if (p != FP32 && p != TF32X3) throw QFX_ERR("Precision mode ", p, " is not available in this build.");
   precision_ = p;
+}
+
+void Engine::set_option(const std::string& name, double value) {
+  if (name == "tc_chunk") {
+    if (!(value >= 1 && value <= 64) || value != double(int(value)))
+      throw QFX_ERR("Option tc_chunk must be an integer in 1..64.");
+    tc_cfg_.chunk = int(value);
+  } else if (name == "tc_pair") {
+    if (value != 0 && value != 1) throw QFX_ERR("Option tc_pair must be 0 or 1.");
+    tc_cfg_.variant = value == 0 ? 0 : -1;
+  } else if (name == "graphs") {
+    if (value != 0 && value != 1) throw QFX_ERR("Option graphs must be 0 or 1.");
+    graphs_ = value != 0;
+  } else if (name == "max_batch") {
+    if (!(value >= 0 && value <= 65535) || value != double(int(value)))
+      throw QFX_ERR("Option max_batch must be an integer in 0..65535.");
+    max_batch_ = int(value);
+  } else {
+    throw QFX_ERR("Unknown option '", name, "'.");
+  }
+  ++options_version_;
+}
+
+double Engine::get_option(const std::string& name) const {
+  if (name == "tc_chunk") return tc_cfg_.chunk;
+  if (name == "tc_pair") return tc_cfg_.variant == 0 ? 0 : 1;
+  if (name == "graphs") return graphs_ ? 1 : 0;
+  if (name == "max_batch") return max_batch_;
+  throw QFX_ERR("Unknown option '", name, "'.");
+}
+
+void Engine::set_tc_variant(std::size_t m, std::size_t n, std::size_t k, int variant) {
+  if (variant < -1 || variant > 1) throw QFX_ERR("Tensor-core variant must be -1, 0 or 1.");
+  if (variant == -1)
+    tc_variant_.erase({m, n, k});
+  else
+    tc_variant_[{m, n, k}] = variant;
+  ++options_version_;
+}
+
+TcConfig Engine::tc_config(std::size_t m, std::size_t n, std::size_t k) const {
+  TcConfig c = tc_cfg_;
+  const auto it = tc_variant_.find({m, n, k});
+  if (it != tc_variant_.end()) c.variant = it->second;
+  return c;
 }
 
 int* Engine::error_flag() { return (int*)reserve(sizeof(int) * 4, 5); }
@@ -140,7 +188,8 @@ void Engine::multiply(const float2* A, const float2* B, float2* C, std::size_t m
       make_perm_plan(nbits, perm, &plan);
       for (int b = 0; b < batch; ++b)
         launch_permute(plan, B + (std::size_t)b * stride, Bt + (std::size_t)b * n * k, 0, 1, stream_);
-      launch_cgemm_tf32x3(A, Bt, C, m, n, k, stride, n * k, batch, ws + 2 * bt, error_flag(), stream_);
+      launch_cgemm_tf32x3(A, Bt, C, m, n, k, stride, n * k, batch, ws + 2 * bt, error_flag(),
+                          tc_config(m, n, k), stream_);
       return;
     }
   }
@@ -292,7 +341,7 @@ std::size_t Engine::run_program(Plan& p, int batch, float2* arena, float* tc_ws)
       launches += 1;
     } else if (op.b_nk) {
       launch_cgemm_tf32x3(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, stride,
-                          batch, tc_ws, err, stream_);
+                          batch, tc_ws, err, tc_config(op.m, op.n, op.k), stream_);
       launches += 3;  // two plane splits and the product
     } else {
       launch_cgemm_fp32(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, batch,
@@ -448,6 +497,7 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
   const std::size_t per_entry = arena_bytes + p.tc_ws_elems * sizeof(float);
   int chunk = (int)std::max<std::size_t>(1, std::min<std::size_t>((std::size_t)total, usable / std::max<std::size_t>(per_entry, 1)));
   chunk = std::min(chunk, 65535);
+  if (max_batch_ > 0) chunk = std::min(chunk, max_batch_);
 
   float2* arena = (float2*)reserve(arena_bytes * (std::size_t)chunk, 0);
   float* tc_ws = p.tc_ws_elems ? tc_workspace(p.tc_ws_elems * (std::size_t)chunk) : nullptr;
@@ -488,7 +538,7 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
     // The whole pass (flatten, program, sums) is one CUDA graph once the
     // same batch size and buffers repeat: the first pass runs eagerly, the
     // second is captured, later ones replay the graph.
-    const GraphKey gk{nb, arena, tc_ws, d_bits, d_amps};
+    const GraphKey gk{nb, arena, tc_ws, d_bits, d_amps, options_version_, precision_};
     if (!profile_ && p.graph && p.graph_key == gk) {
       QFX_CUDA(cudaGraphLaunch(p.graph, stream_));
       launches += p.graph_launches;

@@ -4,11 +4,14 @@
 #include <cuda_runtime.h>
 
 #include <complex>
+#include <map>
+#include <tuple>
 #include <memory>
 #include <string>
 #include <vector>
 
 #include "kernels.h"
+#include "tc_gemm.h"
 #include "planner.h"
 #include "qfx.h"
 
@@ -73,6 +76,13 @@ class Engine {
   // Per-op timing: with profiling on, every device op is bracketed by CUDA
   // events (graph replay is off) and last_ops() reports each op's time.
   void set_profiling(bool on) { profile_ = on; }
+  // Tuning options: "tc_chunk", "tc_pair", "graphs", "max_batch" (see the
+  // C ABI). Unknown names throw.
+  void set_option(const std::string& name, double value);
+  double get_option(const std::string& name) const;
+  // Tensor-core kernel of products of one shape (0 single CTA, 1 CTA pair,
+  // -1 removes the override).
+  void set_tc_variant(std::size_t m, std::size_t n, std::size_t k, int variant);
   std::vector<OpRecord> last_ops() const;
 
   // Device buffers owned by the engine, reused across calls.
@@ -101,6 +111,11 @@ class Engine {
   bool own_stream_ = false;
   bool graphs_ = true;  // capture repeated device passes (QFLEX_GB300_GRAPHS=0 disables)
   bool profile_ = false;
+  TcConfig tc_cfg_;
+  std::map<std::tuple<std::size_t, std::size_t, std::size_t>, int> tc_variant_;
+  int max_batch_ = 0;            // output strings per device pass (0: as many as fit)
+  unsigned options_version_ = 0;  // part of the graph key: options change launches
+  TcConfig tc_config(std::size_t m, std::size_t n, std::size_t k) const;
   std::vector<cudaEvent_t> prof_events_;
   std::vector<double> op_ms_;
   std::unique_ptr<Plan> plan_;

@@ -138,17 +138,35 @@ __global__ void __launch_bounds__(256) permute_kernel(const __grid_constant__ Pe
   const std::uint32_t T = 1u << P.tile_bits;
   const float2* s = src + std::uint64_t(blockIdx.y) * batch_stride;
   float2* d = dst + std::uint64_t(blockIdx.y) * batch_stride;
-  for (std::uint64_t t = blockIdx.x; t < P.n_tiles; t += gridDim.x) {
+  // The next tile's loads are issued into registers before the current
+  // tile is stored, so loads stay in flight through the store phase.
+  float2 r[4];
+  auto load = [&](std::uint64_t t) {
     std::uint64_t bi, bo;
     perm_tile_base(P, t, &bi, &bo);
-#pragma unroll 4
-    for (std::uint32_t j = threadIdx.x; j < T; j += blockDim.x)
-      tile[perm_swizzle(j)] = s[bi + tab[j & 31] + tab[32 + (j >> 5)]];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const std::uint32_t j = threadIdx.x + 256u * i;
+      if (j < T) r[i] = __ldcs(s + bi + tab[j & 31] + tab[32 + (j >> 5)]);
+    }
+  };
+  std::uint64_t t = blockIdx.x;
+  if (t < P.n_tiles) load(t);
+  for (; t < P.n_tiles; t += gridDim.x) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const std::uint32_t j = threadIdx.x + 256u * i;
+      if (j < T) tile[perm_swizzle(j)] = r[i];
+    }
     __syncthreads();
-#pragma unroll 4
-    for (std::uint32_t j = threadIdx.x; j < T; j += blockDim.x)
-      d[bo + tab[64 + (j & 31)] + tab[96 + (j >> 5)]] =
-          tile[perm_swizzle(tab[128 + (j & 31)] + tab[160 + (j >> 5)])];
+    if (t + gridDim.x < P.n_tiles) load(t + gridDim.x);
+    std::uint64_t bi, bo;
+    perm_tile_base(P, t, &bi, &bo);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const std::uint32_t j = threadIdx.x + 256u * i;
+      if (j < T) d[bo + tab[64 + (j & 31)] + tab[96 + (j >> 5)]] = tile[perm_swizzle(tab[128 + (j & 31)] + tab[160 + (j >> 5)])];
+    }
     __syncthreads();
   }
 }
@@ -467,14 +485,25 @@ void make_perm_plan(int R, const std::uint8_t* perm, PermPlan* P) {
       if (in_tile[p] && perm[p] == q) t_out[no++] = p;
   P->tile_bits = (std::uint32_t)nt;
   int n_outer = 0;
+  std::uint8_t outer_in[40], outer_out[40];
   for (int p = 0; p < R; ++p)
     if (!in_tile[p]) {
-      P->outer_in[n_outer] = (std::uint8_t)p;
-      P->outer_out[n_outer] = perm[p];
+      outer_in[n_outer] = (std::uint8_t)p;
+      outer_out[n_outer] = perm[p];
       ++n_outer;
     }
+  if (n_outer > 25) throw std::string("ERROR (qflex_gb300: permute) --> too many digits outside the tile");
   P->n_outer = (std::uint32_t)n_outer;
   P->n_tiles = std::uint64_t(1) << n_outer;
+  for (int g = 0; g < 5; ++g)
+    for (std::uint32_t x = 0; x < 32; ++x)
+      for (int b = 0; b < 5; ++b) {
+        const int q = 5 * g + b;
+        if (q < n_outer && ((x >> b) & 1)) {
+          P->otab[0][g][x] |= 1u << outer_in[q];
+          P->otab[1][g][x] |= 1u << outer_out[q];
+        }
+      }
   for (std::uint32_t j = 0; j < 32; ++j) {
     for (int q = 0; q < 5; ++q) {
       if (!((j >> q) & 1)) continue;

@@ -41,13 +41,16 @@ void launch_flatten(const ColumnDesc* cols, int n_cols, std::uint32_t max_size_l
 // coalesced); the remaining digits index the tiles.
 struct PermPlan {
   std::uint32_t tile_bits;
-  std::uint32_t n_outer;                 // number of digits outside the tile
+  std::uint32_t n_outer;                 // number of digits outside the tile (<= 25)
   std::uint64_t n_tiles;                 // 2^n_outer
-  std::uint8_t outer_in[40], outer_out[40];
   // Lookup tables split by the low / high five bits of a tile index j:
   // [0],[1] input offset of tile element j (input order); [2],[3] output
   // offset of output-order element j; [4],[5] its tile slot.
   std::uint32_t tab[6][32];
+  // Tile base offsets by five-bit groups g of the tile number t:
+  // otab[0][g][x] / otab[1][g][x] = input / output offset contributed by
+  // bits 5g .. 5g+4 of t having the value x.
+  std::uint32_t otab[2][5][32];
 };
 
 void make_perm_plan(int nbits, const std::uint8_t* perm, PermPlan* plan);
@@ -57,11 +60,12 @@ void make_perm_plan(int nbits, const std::uint8_t* perm, PermPlan* plan);
 __host__ __device__ inline std::uint32_t perm_swizzle(std::uint32_t j) { return j ^ ((j >> 5) & 31u); }
 __host__ __device__ inline void perm_tile_base(const PermPlan& P, std::uint64_t t, std::uint64_t* bi,
                                                std::uint64_t* bo) {
-  std::uint64_t i = 0, o = 0;
-  for (std::uint32_t q = 0; q < P.n_outer; ++q) {
-    const std::uint64_t bit = (t >> q) & 1u;
-    i |= bit << P.outer_in[q];
-    o |= bit << P.outer_out[q];
+  std::uint32_t i = 0, o = 0;
+#pragma unroll
+  for (int g = 0; g < 5; ++g) {
+    const std::uint32_t x = std::uint32_t(t >> (5 * g)) & 31u;
+    i += P.otab[0][g][x];
+    o += P.otab[1][g][x];
   }
   *bi = i;
   *bo = o;

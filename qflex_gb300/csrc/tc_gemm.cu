@@ -327,6 +327,268 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
 }
 
+// ---- CTA-pair kernel (cta_group::2) -------------------------------------------
+//
+// Same arithmetic as above on a 256 x 128 output tile shared by the two CTAs
+// of a cluster: CTA r holds A rows m0 + 128 r .. + 127 and B rows (output
+// columns) n0 + 64 r .. + 63 in its shared memory, and one MMA of M = 256,
+// N = 128 issued by the even CTA reads both CTAs' tiles and writes each
+// CTA's 128 rows into that CTA's TMEM. Per k-step an SM now reads 6 KB of
+// operands per MMA (its A rows and half of B) instead of 8 KB, and TMA
+// writes 24 KB instead of 32 KB, which is what bounded the single-CTA tile.
+//
+// Synchronisation across the pair:
+//   * both CTAs' TMA loads complete on the even CTA's full[s] barrier, which
+//     expects the bytes of both;
+//   * MMA commits are multicast to both CTAs (empty[s], acc_full[b],
+//     mma_done), so each CTA's producer and epilogue wait on local barriers;
+//   * both CTAs' epilogue warps arrive on the even CTA's acc_empty[b];
+//   * cluster barriers after set-up (barriers initialised, TMEM allocated)
+//     and before TMEM is released.
+constexpr int PBM = 128;          // rows per CTA (256 per pair)
+constexpr int PBN = 128;          // output columns per pair
+constexpr int PBN_CTA = PBN / 2;  // B rows per CTA
+constexpr int P_STAGES = 8;
+constexpr int P_TILE_A = PBM * 128;
+constexpr int P_TILE_B = PBN_CTA * 128;
+constexpr int P_STAGE_BYTES = P_TILE_A + P_TILE_B;
+constexpr int P_SMEM_BYTES = P_STAGES * P_STAGE_BYTES + 1024 + 256;
+constexpr int P_GROUP = 4;  // pair-row tiles per raster group
+
+__device__ __forceinline__ std::uint32_t cluster_rank() {
+  std::uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// Shared::cluster address of the same shared-memory offset in CTA `rank`.
+__device__ __forceinline__ std::uint32_t peer_addr(const void* p, std::uint32_t rank) {
+  std::uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_test_cluster(std::uint64_t* bar, std::uint32_t parity) {
+  std::uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_cluster(std::uint64_t* bar, std::uint32_t parity, volatile int* abort_flag,
+                                                  int* err, int code) {
+  const unsigned long long t0 = now_ns();
+  while (!mbar_test_cluster(bar, parity)) {
+    if (*abort_flag) return false;
+    if (now_ns() - t0 > WAIT_NS) {
+      *abort_flag = 1;
+      atomicExch(err, code);
+      return false;
+    }
+  }
+  return true;
+}
+__device__ __forceinline__ void mbar_arrive_remote(std::uint32_t cluster_addr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
+}
+// TMA load into this CTA's shared memory that completes on a barrier of
+// either CTA of the pair (`bar` is a shared::cluster address).
+__device__ __forceinline__ void tma_load_4d_pair(const CUtensorMap* map, std::uint32_t bar, void* dst, int c0, int c1,
+                                                 int c2, int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+      "%4, %5}], [%6];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<std::uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void umma_tf32_pair(std::uint32_t d_tmem, std::uint64_t a, std::uint64_t b,
+                                               std::uint32_t idesc, std::uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+// Commit of the issuing thread's MMAs, arriving on `bar` in both CTAs.
+__device__ __forceinline__ void umma_commit_pair(std::uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "h"(std::uint16_t(3))
+      : "memory");
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
+    cgemm_tf32x3_pair_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                             float2* __restrict__ C, int m, int n, int k, std::uint64_t c_batch_stride,
+                             int* __restrict__ err, int CHUNK) {
+  extern __shared__ __align__(1024) std::uint8_t smem_raw[];
+  std::uint8_t* smem = reinterpret_cast<std::uint8_t*>((reinterpret_cast<std::uintptr_t>(smem_raw) + 1023) &
+                                                       ~std::uintptr_t(1023));
+  std::uint64_t* full = reinterpret_cast<std::uint64_t*>(smem + P_STAGES * P_STAGE_BYTES);
+  std::uint64_t* empty = full + P_STAGES;
+  std::uint64_t* acc_full = empty + P_STAGES;
+  std::uint64_t* acc_empty = acc_full + 2;  // used in the even CTA only
+  std::uint64_t* mma_done = acc_empty + 2;
+  std::uint32_t* tmem_slot = reinterpret_cast<std::uint32_t*>(mma_done + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const std::uint32_t rank = cluster_rank();
+  const int pair = blockIdx.x / 2;
+  const int tiles_m = (m + 2 * PBM - 1) / (2 * PBM);
+  const int tiles_n = (n + PBN - 1) / PBN;
+  const int per_group = P_GROUP * tiles_n;
+  const int group = pair / per_group, in_group = pair % per_group;
+  const int group_m = min(P_GROUP, tiles_m - group * P_GROUP);
+  const int m0 = (group * P_GROUP + in_group % group_m) * (2 * PBM) + int(rank) * PBM;
+  const int n0 = (in_group / group_m) * PBN;
+  const int batch = blockIdx.z;
+  const int kblocks = (k + BK - 1) / BK;
+  const int chunks = (kblocks + CHUNK - 1) / CHUNK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < P_STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 2 * EPI_WARPS);
+    }
+    mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  cluster_sync();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const std::uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // Producer (both CTAs): this CTA's A rows and B rows, completing on the
+    // even CTA's full barrier.
+    int issued = 0;
+    for (int kb = 0; kb < kblocks; ++kb) {
+      const int s = kb % P_STAGES;
+      if (kb >= P_STAGES && !mbar_wait_cluster(&empty[s], ((kb / P_STAGES) - 1) & 1, abort_flag, err, 11)) break;
+      std::uint8_t* st = smem + s * P_STAGE_BYTES;
+      if (rank == 0) mbar_expect_tx(&full[s], 2 * P_STAGE_BYTES);
+      const std::uint32_t bar = peer_addr(&full[s], 0);
+      tma_load_4d_pair(&map_a, bar, st, 0, kb, m0, batch);
+      tma_load_4d_pair(&map_b, bar, st + P_TILE_A, 0, kb, n0 + int(rank) * PBN_CTA, batch);
+      issued = kb + 1;
+    }
+    if (*abort_flag && rank == 0) {
+      for (int kb = issued > P_STAGES ? issued - P_STAGES : 0; kb < issued; ++kb) {
+        const unsigned long long t0 = now_ns();
+        while (!mbar_test_cluster(&full[kb % P_STAGES], (kb / P_STAGES) & 1) && now_ns() - t0 < WAIT_NS) {
+        }
+      }
+    }
+  } else if (warp == 1 && lane == 0 && rank == 0) {
+    // MMA issuer of the pair (even CTA).
+    const std::uint32_t idp = idesc_tf32(2 * PBM, PBN, false), idn = idesc_tf32(2 * PBM, PBN, true);
+    for (int kb = 0; kb < kblocks; ++kb) {
+      const int s = kb % P_STAGES;
+      const int c = kb / CHUNK, buf = c & 1;
+      const bool first = kb % CHUNK == 0;
+      if (first && c >= 2 && !mbar_wait_cluster(&acc_empty[buf], ((c >> 1) - 1) & 1, abort_flag, err, 14)) break;
+      if (!mbar_wait_cluster(&full[s], (kb / P_STAGES) & 1, abort_flag, err, 12)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const std::uint32_t d_re = tmem + buf * 2 * PBN, d_im = d_re + PBN;
+      const std::uint32_t a0 = smem_u32(smem + s * P_STAGE_BYTES);
+      const std::uint32_t b0 = a0 + P_TILE_A;
+      const std::uint64_t arh = smem_desc_sw128(a0), arl = smem_desc_sw128(a0 + 32),
+                          aih = smem_desc_sw128(a0 + 64), ail = smem_desc_sw128(a0 + 96);
+      const std::uint64_t brh = smem_desc_sw128(b0), brl = smem_desc_sw128(b0 + 32),
+                          bih = smem_desc_sw128(b0 + 64), bil = smem_desc_sw128(b0 + 96);
+      const std::uint32_t acc = first ? 0u : 1u;
+      umma_tf32_pair(d_re, arh, brl, idp, acc);
+      umma_tf32_pair(d_re, arl, brh, idp, 1);
+      umma_tf32_pair(d_re, aih, bil, idn, 1);
+      umma_tf32_pair(d_re, ail, bih, idn, 1);
+      umma_tf32_pair(d_re, arh, brh, idp, 1);
+      umma_tf32_pair(d_re, aih, bih, idn, 1);
+      umma_tf32_pair(d_im, arh, bil, idp, acc);
+      umma_tf32_pair(d_im, arl, bih, idp, 1);
+      umma_tf32_pair(d_im, aih, brl, idp, 1);
+      umma_tf32_pair(d_im, ail, brh, idp, 1);
+      umma_tf32_pair(d_im, arh, bih, idp, 1);
+      umma_tf32_pair(d_im, aih, brh, idp, 1);
+      umma_commit_pair(&empty[s]);
+      if (kb % CHUNK == CHUNK - 1 || kb == kblocks - 1) umma_commit_pair(&acc_full[buf]);
+    }
+    umma_commit_pair(mma_done);
+  } else if (warp >= 2) {
+    // Epilogue (both CTAs): this CTA's 128 rows from its own TMEM.
+    const int q = warp % 4;
+    const int half = (warp - 2) / 4;
+    const int row = q * 32 + lane;
+    const std::uint32_t empty0 = peer_addr(&acc_empty[0], 0), empty1 = peer_addr(&acc_empty[1], 0);
+    float tre[PBN / 2], tim[PBN / 2];
+#pragma unroll
+    for (int j = 0; j < PBN / 2; ++j) tre[j] = tim[j] = 0.f;
+    bool ok = true;
+    for (int c = 0; c < chunks; ++c) {
+      const int buf = c & 1;
+      if (!mbar_wait_cluster(&acc_full[buf], (c >> 1) & 1, abort_flag, err, 13)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const std::uint32_t base = tmem + (std::uint32_t(q * 32) << 16) + buf * 2 * PBN + half * (PBN / 2);
+#pragma unroll
+      for (int j0 = 0; j0 < PBN / 2; j0 += 32) {
+        std::uint32_t vr[32], vi[32];
+        TMEM_LD32(base + j0, vr);
+        TMEM_LD32(base + PBN + j0, vi);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          tre[j0 + j] += __uint_as_float(vr[j]);
+          tim[j0 + j] += __uint_as_float(vi[j]);
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncwarp();
+      if (lane == 0) mbar_arrive_remote(buf ? empty1 : empty0);
+    }
+    if (ok && m0 + row < m) {
+      float2* crow =
+          C + std::uint64_t(batch) * c_batch_stride + std::uint64_t(m0 + row) * n + n0 + half * (PBN / 2);
+      const int ncols = n - n0 - half * (PBN / 2);
+#pragma unroll
+      for (int j = 0; j < PBN / 2; ++j)
+        if (j < ncols) crow[j] = make_float2(tre[j], tim[j]);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 1) {
+    // Every MMA of the pair has completed before either CTA frees TMEM or
+    // leaves (the MMAs read both CTAs' shared memory).
+    const unsigned long long t0 = now_ns();
+    while (!mbar_test_cluster(mma_done, 0) && now_ns() - t0 < WAIT_NS) {
+    }
+  }
+  __syncthreads();
+  cluster_sync();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+  }
+}
+
 // Splits complex64 rows into the four TF32 planes (round-to-nearest).
 __device__ __forceinline__ float tf32_rn(float x) {
   std::uint32_t r;
@@ -404,20 +666,29 @@ std::size_t tc_workspace_elems(std::size_t m, std::size_t n, std::size_t k) {
   return 4 * (m + n) * ((k + 7) / 8 * 8);
 }
 
+TcConfig tc_default_config() {
+  TcConfig c;
+  // k-steps per TMEM chunk. Measured on the 7x7 (1+32+1) network (8
+  // amplitudes vs FP64): 1 -> max 1.0e-5 at 8.9 amplitudes/s, 2 -> max
+  // 8.7e-6 at 9.8, 4 -> max 1.6e-5 at 10.4.
+  if (const char* e = std::getenv("QFLEX_TC_CHUNK")) {
+    const int v = std::atoi(e);
+    if (v >= 1 && v <= 64) c.chunk = v;
+  }
+  if (const char* e = std::getenv("QFLEX_TC_PAIR"))
+    if (std::atoi(e) == 0) c.variant = 0;
+  return c;
+}
+
 void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size_t m, std::size_t n,
                          std::size_t k, std::uint64_t batch_stride, std::uint64_t bt_stride, int batch,
-                         float* workspace, int* err, cudaStream_t s) {
+                         float* workspace, int* err, const TcConfig& cfg, cudaStream_t s) {
   if (!tc_eligible(m, n, k)) throw std::string("ERROR (qflex_gb300: tensor cores) --> shape not eligible");
-  static const int chunk = [] {
-    // k-steps per TMEM chunk. Measured on the 7x7 (1+32+1) network (8
-    // amplitudes vs FP64): 1 -> max 1.0e-5 at 8.9 amplitudes/s, 2 -> max
-    // 8.7e-6 at 9.8, 4 -> max 1.6e-5 at 10.4. QFLEX_TC_CHUNK overrides 2.
-    const char* e = std::getenv("QFLEX_TC_CHUNK");
-    const int c = e ? std::atoi(e) : 2;
-    return c >= 1 ? c : 2;
-  }();
-  // Epilogue warps poll the chunk barrier with this back-off (0: plain
-  // bounded wait); QFLEX_TC_EPI_SLEEP_NS overrides.
+  if (cfg.chunk < 1 || cfg.chunk > 64)
+    throw std::string("ERROR (qflex_gb300: tensor cores) --> chunk length must be 1..64");
+  const int chunk = cfg.chunk;
+  // Epilogue warps of the single-CTA kernel poll the chunk barrier with
+  // this back-off (0: plain bounded wait); QFLEX_TC_EPI_SLEEP_NS overrides.
   static const int epi_sleep = [] {
     const char* e = std::getenv("QFLEX_TC_EPI_SLEEP_NS");
     return e ? std::atoi(e) : 0;
@@ -426,7 +697,11 @@ void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size
   std::call_once(attr, [] {
     check(cudaFuncSetAttribute(cgemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
           "cudaFuncSetAttribute");
+    check(cudaFuncSetAttribute(cgemm_tf32x3_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               P_SMEM_BYTES),
+          "cudaFuncSetAttribute");
   });
+  const bool use_pair = cfg.variant == 1 || (cfg.variant < 0 && m >= 2 * PBM);
   float* pa = workspace;
   const std::size_t kpad = (k + BK - 1) / BK * BK;
   float* pb = workspace + 4 * m * kpad * (std::size_t)batch;
@@ -436,6 +711,16 @@ void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size
     dim3 gb((unsigned)std::min<std::uint64_t>((n * k + 255) / 256, 152 * 16), (unsigned)batch);
     split_tf32_kernel<<<gb, 256, 0, s>>>(Bt, pb, n, k, kpad, bt_stride);
     check(cudaGetLastError(), "split_tf32");
+  }
+  if (use_pair) {
+    const CUtensorMap ma = plane_map(pa, m, kpad, batch, PBM);
+    const CUtensorMap mb = plane_map(pb, n, kpad, batch, PBN_CTA);
+    const std::size_t pairs = ((m + 2 * PBM - 1) / (2 * PBM)) * ((n + PBN - 1) / PBN);
+    dim3 grid((unsigned)(2 * pairs), 1, (unsigned)batch);
+    cgemm_tf32x3_pair_kernel<<<grid, THREADS, P_SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride,
+                                                                 err, chunk);
+    check(cudaGetLastError(), "cgemm_tf32x3_pair");
+    return;
   }
   const CUtensorMap ma = plane_map(pa, m, kpad, batch, BM);
   const CUtensorMap mb = plane_map(pb, n, kpad, batch, BN);

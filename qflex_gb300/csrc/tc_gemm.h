@@ -14,6 +14,14 @@ bool tc_eligible(std::size_t m, std::size_t n, std::size_t k);
 // fp32 elements of split planes one batch entry needs (A and B, 4 planes).
 std::size_t tc_workspace_elems(std::size_t m, std::size_t n, std::size_t k);
 
+// Kernel choice of one product.
+struct TcConfig {
+  int chunk = 2;     // k-steps (of 8) per TMEM accumulation chunk, 1..64
+  int variant = -1;  // -1: CTA pair when m >= 256, else single; 0: single CTA; 1: CTA pair
+};
+// Defaults: chunk from QFLEX_TC_CHUNK, variant 0 when QFLEX_TC_PAIR=0.
+TcConfig tc_default_config();
+
 // C[m,n] = A[m,k] * Bt[n,k]^T (complex64, both K-major), 3xTF32 split,
 // FP32 accumulation. Batch entry b reads A + b * ac_stride,
 // Bt + b * bt_stride and writes C + b * ac_stride. `workspace` holds
@@ -21,6 +29,6 @@ std::size_t tc_workspace_elems(std::size_t m, std::size_t n, std::size_t k);
 // code if a pipeline wait expired.
 void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size_t m, std::size_t n,
                          std::size_t k, std::uint64_t ac_stride, std::uint64_t bt_stride, int batch,
-                         float* workspace, int* err, cudaStream_t s);
+                         float* workspace, int* err, const TcConfig& cfg, cudaStream_t s);
 
 }  // namespace qfx

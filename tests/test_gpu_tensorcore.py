@@ -19,8 +19,11 @@ def tc_ctx(built_lib):
     return Context(0, TF32X3)
 
 
+# m < 256 runs on the single-CTA kernel, m >= 256 on the CTA-pair kernel;
+# ragged m and n leave whole CTAs of a pair outside the matrix.
 @pytest.mark.parametrize("m,n,k", [(128, 128, 16), (64, 64, 16), (256, 512, 128), (1024, 256, 256),
-                                   (300, 128, 64), (128, 1024, 40), (4096, 256, 256)])
+                                   (300, 128, 64), (128, 1024, 40), (4096, 256, 256), (256, 64, 16),
+                                   (512, 96, 24), (768, 200, 100), (2048, 2048, 2048)])
 def test_tf32x3_multiply(tc_ctx, m, n, k):
     import torch
     g = np.random.default_rng(m + 7 * n + 13 * k)

@@ -1,0 +1,79 @@
+"""Tuning options of a context and the autotuner: option validation and
+the tensor-core shape list on CPU (planning-only context); on the GPU,
+results that do not depend on the kernel variant, graph replay or the
+strings-per-pass limit, and an autotuning run."""
+import numpy as np
+import pytest
+
+from qflex_gb300 import TF32X3, Context, QflexGb300Error, autotune, rqc
+from tests.conftest import rel_err
+
+
+def test_options_round_trip_and_validation(built_lib):
+    c = Context(-1, TF32X3)
+    assert c.get_option("tc_chunk") >= 1
+    for name, value in (("tc_chunk", 4), ("tc_pair", 0), ("graphs", 0), ("max_batch", 3)):
+        c.set_option(name, value)
+        assert c.get_option(name) == value
+    for name, value in (("tc_chunk", 0), ("tc_chunk", 65), ("tc_chunk", 1.5), ("tc_pair", 2),
+                        ("graphs", -1), ("max_batch", -1), ("no_such_option", 1)):
+        with pytest.raises(QflexGb300Error):
+            c.set_option(name, value)
+    with pytest.raises(QflexGb300Error):
+        c.get_option("no_such_option")
+    c.set_tc_variant(4096, 4096, 4096, 1)
+    c.set_tc_variant(4096, 4096, 4096, -1)
+    with pytest.raises(QflexGb300Error):
+        c.set_tc_variant(64, 64, 64, 2)
+
+
+def test_tc_shapes_of_7x7_plan(built_lib):
+    circuit, ordering, grid, _, _ = rqc.workload("c3")
+    shapes = autotune.tc_shapes(circuit, ordering, grid)
+    assert shapes[0] == (4096, 4096, 4096, 20)
+    assert (65536, 256, 256, 109) in shapes
+    assert all(autotune.tc_eligible(m, n, k) for m, n, k, _ in shapes)
+    flops = [m * n * k * c for m, n, k, c in shapes]
+    assert flops == sorted(flops, reverse=True)
+
+
+@pytest.mark.gpu
+def test_variants_graphs_and_batches_agree(built_lib):
+    circuit, ordering, grid, initial, finals = rqc.workload("c2")
+    finals = finals[:6]
+    ctx = Context(0, TF32X3)
+    base = [a for _, a in ctx.evaluate_many(circuit, ordering, grid, initial, finals, 1 << 40)]
+    shapes = autotune.tc_shapes(circuit, ordering, grid)
+    assert shapes
+    for variant in (0, 1):
+        for m, n, k, _ in shapes:
+            ctx.set_tc_variant(m, n, k, variant)
+        for _ in range(3):  # eager, captured, replayed
+            got = [a for _, a in ctx.evaluate_many(circuit, ordering, grid, initial, finals, 1 << 40)]
+            assert rel_err(got, base) < 1e-5, variant
+    ctx.set_option("graphs", 0)
+    ctx.set_option("max_batch", 4)  # 6 strings -> passes of 4 and 2
+    got = [a for _, a in ctx.evaluate_many(circuit, ordering, grid, initial, finals, 1 << 40)]
+    assert rel_err(got, base) < 1e-5
+    assert ctx.stats()["batch"] == 4
+
+
+@pytest.mark.gpu
+def test_autotune_sets_choices(built_lib, tmp_path):
+    import torch
+    circuit, ordering, grid, initial, finals = rqc.workload("c2")
+    finals = finals[:4]
+    ctx = Context(0, TF32X3)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    cache = tmp_path / "tune.json"
+    res = autotune.tune(ctx, circuit, ordering, grid, initial, finals, batches=(1, 2, 4), cache=cache,
+                        stream=stream)
+    assert not res["cached"] and res["max_batch"] in (1, 2, 4)
+    assert res["products"] and all(r["variant"] in (0, 1) for r in res["products"].values())
+    assert ctx.get_option("max_batch") == res["max_batch"]
+    again = autotune.tune(Context(0, TF32X3), circuit, ordering, grid, initial, finals, batches=(1, 2, 4),
+                          cache=cache, stream=stream)
+    assert again["cached"] and again["max_batch"] == res["max_batch"]
+    out = ctx.evaluate_many(circuit, ordering, grid, initial, finals, 1 << 40)
+    assert np.isfinite([abs(a) for _, a in out]).all()
