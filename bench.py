@@ -37,6 +37,9 @@ METRIC = "amplitudes/s on 7x7 1+32+1 RQC; split-precision vs FP32, rel err≤1e-
 UNIT = "amplitudes/s"
 WORKLOAD = "c3"
 FP32_PEAK_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12  # TFLOP/s, FP32 CUDA-core FMA
+# DRAM bytes (read + write) of one launch of the dominant product, from ncu
+# captures summarised in profiles/.
+TRAFFIC = {("tf32x3", 4096, 4096, 4096): 2.322e9}
 
 
 def parse():
@@ -46,7 +49,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--batch", type=int, default=8, help="output strings per step")
     p.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    p.add_argument("--precision", default="tf32x3", choices=["tf32x3", "fp32"])
+    p.add_argument("--precision", default="fp16x3", choices=["fp16x3", "tf32x3", "fp32"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-autotune", action="store_true",
                    help="skip the tensor-core kernel / strings-per-pass autotuning before warm-up")
@@ -254,12 +257,14 @@ def main():
         return [finals[(base + i) % len(finals)] for i in range(B)]
 
     tuned = None
-    if args.precision == "tf32x3" and not args.no_autotune:
-        # Untimed: kernel variant per product shape, strings per device pass
-        # (on strings from the end of the list, not used by the steps).
+    if args.precision != "fp32" and not args.no_autotune:
+        # Untimed: kernel variant per product shape (3xTF32 only), strings
+        # per device pass (on strings from the end of the list, not used by
+        # the steps).
         from qflex_gb300 import autotune
         tuned = autotune.tune(ctx, circuit, ordering, grid, initial, finals[-B:],
-                              batches=[b for b in (1, 2, 4, 8, 16) if b <= B], stream=stream)
+                              batches=[b for b in (1, 2, 4, 8, 16) if b <= B], stream=stream,
+                              products=args.precision == "tf32x3")
     for w in range(args.warmup):
         ctx.evaluate_many(circuit, ordering, grid, initial, strings(w), 1 << 40)
     with ClockSampler(local) as clocks:
@@ -309,31 +314,36 @@ def main():
                                "the measured peaks hold no FP32 CUDA-core figure",
                 "traffic": None, "timing": "CUDA events, dominant shape, 5 launches"}
         else:
-            # 3xTF32 with 4 real products = 12 TF32 MMAs of 2mnk per 8mnk of
-            # algorithmic work; the TF32 dense rate is half the bf16 rate.
+            # Split products with 4 real products x 3 terms = 12 MMAs of 2mnk
+            # per 8mnk of algorithmic work. TF32 runs at half the bf16 rate,
+            # FP16 at the bf16 rate.
             bf16 = pk.get("bf16_tflops", 1900.0)
-            tf32_peak = bf16 / 2
+            fp16 = args.precision == "fp16x3"
+            mma_peak = bf16 if fp16 else bf16 / 2
+            src = "measured bf16 dense burst" if "bf16_tflops" in pk else "fallback 1.9 PFLOP/s bf16"
             line["roofline"] = {
-                "bound": "tensor", "kernel": f"cgemm_tf32x3 ({m},{n},{k}) incl. plane splits",
-                "achieved": 3.0 * achieved, "achieved_algorithmic": achieved, "peak": tf32_peak,
-                "unit": "TFLOP/s (TF32 MMA)", "frac": 3.0 * achieved / tf32_peak,
-                "peak_source": ("measured bf16 dense burst / 2 (MEASURED_PEAKS.json)" if "bf16_tflops" in pk
-                                else "fallback 1.9 PFLOP/s bf16 / 2"),
-                "traffic": 2.322e9 if (m, n, k) == (4096, 4096, 4096) else None,
-                "traffic_source": "ncu dram__bytes_read+write of one (4096,4096,4096) launch, "
-                                  "profiles/tc_gemm_4096.md",
+                "bound": "tensor", "kernel": f"cgemm_{args.precision} ({m},{n},{k}) incl. plane splits",
+                "achieved": 3.0 * achieved, "achieved_algorithmic": achieved, "peak": mma_peak,
+                "unit": "TFLOP/s (FP16 MMA)" if fp16 else "TFLOP/s (TF32 MMA)", "frac": 3.0 * achieved / mma_peak,
+                "peak_source": src + (" (MEASURED_PEAKS.json)" if "bf16_tflops" in pk else "") + ("" if fp16 else " / 2"),
+                "traffic": TRAFFIC.get((args.precision, m, n, k)),
+                "traffic_source": "ncu dram__bytes_read+write of one launch of this shape (profiles/)",
                 "timing": "CUDA events on the context stream, dominant shape, 5 launches"}
-            fp = Context(local)
-            fp.set_precision("fp32")
-            fp.set_stream(stream.cuda_stream)
-            fp.evaluate_many(circuit, ordering, grid, initial, strings(0), 1 << 40)
-            f_dev, _ = timed_steps(fp, torch, stream, circuit, ordering, grid, initial, strings,
-                                   args.warmup, 1)
-            fp32_value = B / (f_dev / 1000.0)
-            line["fp32_path"] = {"value": fp32_value, "unit": UNIT, "steps": 1,
-                                 "speedup_of_this_path": value / fp32_value,
-                                 "accuracy": accuracy_vs_fp64(fp, circuit, ordering, grid, initial)}
-            fp.close()
+            # The other paths on the same workload, one step each (after a
+            # warm-up step): the plain FP32 CUDA-core path the metric compares
+            # against, and the other split-precision mode.
+            for other in [q for q in ("fp32", "tf32x3", "fp16x3") if q != args.precision]:
+                fp = Context(local)
+                fp.set_precision(other)
+                fp.set_stream(stream.cuda_stream)
+                fp.evaluate_many(circuit, ordering, grid, initial, strings(0), 1 << 40)
+                f_dev, _ = timed_steps(fp, torch, stream, circuit, ordering, grid, initial, strings,
+                                       args.warmup, 1)
+                o_value = B / (f_dev / 1000.0)
+                line[f"{other}_path"] = {"value": o_value, "unit": UNIT, "steps": 1,
+                                         "speedup_of_this_path": value / o_value,
+                                         "accuracy": accuracy_vs_fp64(fp, circuit, ordering, grid, initial)}
+                fp.close()
         if not args.no_cpu_baseline:
             dt, v, desc, cores = cpu_sample()
             line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",

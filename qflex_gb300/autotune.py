@@ -102,9 +102,9 @@ def tune_batch(ctx: Context, circuit: str, ordering: str, grid: str, initial: st
 
 def tune(ctx: Context, circuit: str, ordering: str, grid: str, initial: str, finals: Sequence[str],
          memory_limit: float = float(1 << 40), batches: Sequence[int] = (1, 2, 4, 8, 16),
-         cache: Optional[Path] = None, stream=None) -> dict:
-    """Tunes `ctx` for this workload (products first, then strings per
-    pass) and returns the choices. `stream` is the torch stream the context
+         cache: Optional[Path] = None, stream=None, products: bool = True) -> dict:
+    """Tunes `ctx` for this workload (products first unless `products` is
+    False, then strings per pass) and returns the choices. `stream` is the torch stream the context
     runs on (a new one is set on the context when None). With `cache`, a
     result stored for the same GPU and product shapes is applied instead of
     measured again."""
@@ -123,7 +123,7 @@ def tune(ctx: Context, circuit: str, ordering: str, grid: str, initial: str, fin
         if key in store:
             apply(ctx, store[key])
             return dict(store[key], cached=True)
-    result = {"products": tune_products(ctx, stream, shapes)}
+    result = {"products": tune_products(ctx, stream, shapes) if products else {}}
     result.update(tune_batch(ctx, circuit, ordering, grid, initial, finals, memory_limit, batches))
     if cache is not None:
         store[key] = result

@@ -17,7 +17,7 @@
 
 namespace qfx {
 
-enum Precision : int { FP32 = 0, TF32X3 = 1, BF16X3 = 2 };
+enum Precision : int { FP32 = 0, TF32X3 = 1, BF16X3 = 2, FP16X3 = 3 };
 
 struct EvalResult {
   std::string initial_state;  // as mutated by EvaluateCircuit

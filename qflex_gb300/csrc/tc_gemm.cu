@@ -32,6 +32,7 @@
 // frees its TMEM before returning.
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <cuda_fp16.h>
 
 #include <cstdlib>
 #include <cstring>
@@ -134,6 +135,34 @@ __device__ __forceinline__ void umma_tf32(std::uint32_t d_tmem, std::uint64_t a,
       " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
       "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
 }
+// Instruction descriptor, kind::f16 with FP16 A and B (format 0), F32 D.
+__host__ __device__ constexpr std::uint32_t idesc_f16(int m, int n, bool negate_a) {
+  return (1u << 4) | (negate_a ? (1u << 13) : 0u) | (std::uint32_t(n >> 3) << 17) | (std::uint32_t(m >> 4) << 24);
+}
+__device__ __forceinline__ void umma_f16(std::uint32_t d_tmem, std::uint64_t a, std::uint64_t b, std::uint32_t idesc,
+                                         std::uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+// Operand kinds of the single-CTA kernel: 3xTF32 planes (8 values of 4
+// bytes per plane and k-step) or 3xFP16 planes (16 values of 2 bytes, rows
+// scaled by powers of two).
+enum SplitKind : int { KIND_TF32 = 0, KIND_FP16 = 1 };
+template <int KIND>
+__device__ __forceinline__ void umma(std::uint32_t d, std::uint64_t a, std::uint64_t b, std::uint32_t id,
+                                     std::uint32_t acc) {
+  if (KIND == KIND_TF32)
+    umma_tf32(d, a, b, id, acc);
+  else
+    umma_f16(d, a, b, id, acc);
+}
+template <int KIND>
+__host__ __device__ constexpr std::uint32_t idesc_kind(int m, int n, bool negate_a) {
+  return KIND == KIND_TF32 ? idesc_tf32(m, n, negate_a) : idesc_f16(m, n, negate_a);
+}
+
 __device__ __forceinline__ void umma_commit(std::uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                    smem_u32(bar))
@@ -155,10 +184,15 @@ __device__ __forceinline__ void mbar_arrive(std::uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-__global__ void __launch_bounds__(THREADS, 1)
-    cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
-                        float2* __restrict__ C, int m, int n, int k, std::uint64_t c_batch_stride,
-                        int* __restrict__ err, int CHUNK, int epi_sleep_ns) {
+// The single-CTA kernel body. KIND_FP16 operands carry per-row scale
+// exponents (value = plane value * 2^-e); the epilogue removes them.
+template <int KIND>
+__device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const CUtensorMap* map_b,
+                                                 float2* __restrict__ C, int m, int n, int k,
+                                                 std::uint64_t c_batch_stride, int* __restrict__ err, int CHUNK,
+                                                 int epi_sleep_ns, const int* __restrict__ exp_a,
+                                                 const int* __restrict__ exp_b) {
+  constexpr int KSTEP = KIND == KIND_TF32 ? 8 : 16;  // k values per plane row of 32 bytes
   extern __shared__ __align__(1024) std::uint8_t smem_raw[];
   std::uint8_t* smem = reinterpret_cast<std::uint8_t*>((reinterpret_cast<std::uintptr_t>(smem_raw) + 1023) &
                                                        ~std::uintptr_t(1023));
@@ -181,7 +215,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int m0 = (group * 8 + in_group % group_m) * BM;
   const int n0 = (in_group / group_m) * BN;
   const int batch = blockIdx.z;
-  const int kblocks = (k + BK - 1) / BK;
+  const int kblocks = (k + KSTEP - 1) / KSTEP;
   const int chunks = (kblocks + CHUNK - 1) / CHUNK;
 
   if (threadIdx.x == 0) {
@@ -215,8 +249,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) - 1) & 1, abort_flag, err, 1)) break;
       std::uint8_t* st = smem + s * STAGE_BYTES;
       mbar_expect_tx(&full[s], STAGE_BYTES);
-      tma_load_4d(&map_a, &full[s], st, 0, kb, m0, batch);
-      tma_load_4d(&map_b, &full[s], st + TILE_A, 0, kb, n0, batch);
+      tma_load_4d(map_a, &full[s], st, 0, kb, m0, batch);
+      tma_load_4d(map_b, &full[s], st + TILE_A, 0, kb, n0, batch);
       issued = kb + 1;
     }
     if (*abort_flag) {
@@ -232,7 +266,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     // MMA issuer. Planes in a stage: A re_hi, re_lo, im_hi, im_lo, then B.
     // Chunk c (CHUNK k-steps) accumulates from zero into TMEM buffer c % 2;
     // the epilogue warps add it into their FP32 registers and free it.
-    const std::uint32_t idp = idesc_tf32(BM, BN, false), idn = idesc_tf32(BM, BN, true);
+    const std::uint32_t idp = idesc_kind<KIND>(BM, BN, false), idn = idesc_kind<KIND>(BM, BN, true);
     for (int kb = 0; kb < kblocks; ++kb) {
       const int s = kb % STAGES;
       const int c = kb / CHUNK, buf = c & 1;
@@ -250,18 +284,18 @@ __global__ void __launch_bounds__(THREADS, 1)
       // The small hi*lo terms go first and the two large hi*hi terms last,
       // so only those two additions round against a large accumulator.
       const std::uint32_t acc = first ? 0u : 1u;
-      umma_tf32(d_re, arh, brl, idp, acc);
-      umma_tf32(d_re, arl, brh, idp, 1);
-      umma_tf32(d_re, aih, bil, idn, 1);
-      umma_tf32(d_re, ail, bih, idn, 1);
-      umma_tf32(d_re, arh, brh, idp, 1);
-      umma_tf32(d_re, aih, bih, idn, 1);
-      umma_tf32(d_im, arh, bil, idp, acc);
-      umma_tf32(d_im, arl, bih, idp, 1);
-      umma_tf32(d_im, aih, brl, idp, 1);
-      umma_tf32(d_im, ail, brh, idp, 1);
-      umma_tf32(d_im, arh, bih, idp, 1);
-      umma_tf32(d_im, aih, brh, idp, 1);
+      umma<KIND>(d_re, arh, brl, idp, acc);
+      umma<KIND>(d_re, arl, brh, idp, 1);
+      umma<KIND>(d_re, aih, bil, idn, 1);
+      umma<KIND>(d_re, ail, bih, idn, 1);
+      umma<KIND>(d_re, arh, brh, idp, 1);
+      umma<KIND>(d_re, aih, bih, idn, 1);
+      umma<KIND>(d_im, arh, bil, idp, acc);
+      umma<KIND>(d_im, arl, bih, idp, 1);
+      umma<KIND>(d_im, aih, brl, idp, 1);
+      umma<KIND>(d_im, ail, brh, idp, 1);
+      umma<KIND>(d_im, arh, bih, idp, 1);
+      umma<KIND>(d_im, aih, brh, idp, 1);
       umma_commit(&empty[s]);
       if (kb % CHUNK == CHUNK - 1 || kb == kblocks - 1) umma_commit(&acc_full[buf]);
     }
@@ -309,9 +343,21 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (ok && m0 + row < m) {
       float2* crow = C + std::uint64_t(batch) * c_batch_stride + std::uint64_t(m0 + row) * n + n0 + half * (BN / 2);
       const int ncols = n - n0 - half * (BN / 2);
+      if (KIND == KIND_FP16) {
+        // Undo the row scales of A (this row) and B (each column).
+        const int ea = exp_a[std::uint64_t(batch) * m + m0 + row];
+        const int* eb = exp_b + std::uint64_t(batch) * n + n0 + half * (BN / 2);
 #pragma unroll
-      for (int j = 0; j < BN / 2; ++j)
-        if (j < ncols) crow[j] = make_float2(tre[j], tim[j]);
+        for (int j = 0; j < BN / 2; ++j)
+          if (j < ncols) {
+            const int e = -(ea + eb[j]);
+            crow[j] = make_float2(ldexpf(tre[j], e), ldexpf(tim[j], e));
+          }
+      } else {
+#pragma unroll
+        for (int j = 0; j < BN / 2; ++j)
+          if (j < ncols) crow[j] = make_float2(tre[j], tim[j]);
+      }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -325,6 +371,21 @@ __global__ void __launch_bounds__(THREADS, 1)
     asm volatile("tcgen05.fence::after_thread_sync;");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
   }
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                        float2* __restrict__ C, int m, int n, int k, std::uint64_t c_batch_stride,
+                        int* __restrict__ err, int CHUNK, int epi_sleep_ns) {
+  cgemm_split_body<KIND_TF32>(&map_a, &map_b, C, m, n, k, c_batch_stride, err, CHUNK, epi_sleep_ns, nullptr, nullptr);
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    cgemm_fp16x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                        float2* __restrict__ C, int m, int n, int k, std::uint64_t c_batch_stride,
+                        int* __restrict__ err, int CHUNK, int epi_sleep_ns, const int* __restrict__ exp_a,
+                        const int* __restrict__ exp_b) {
+  cgemm_split_body<KIND_FP16>(&map_a, &map_b, C, m, n, k, c_batch_stride, err, CHUNK, epi_sleep_ns, exp_a, exp_b);
 }
 
 // ---- CTA-pair kernel (cta_group::2) -------------------------------------------
@@ -618,6 +679,52 @@ __global__ void __launch_bounds__(256) split_tf32_kernel(const float2* __restric
   }
 }
 
+// 3xFP16 planes. One warp per row: the row's largest |re| or |im| sets a
+// power-of-two scale e with max * 2^e in [2^14, 2^15) (FP16 holds up to
+// 65504), then hi = fp16(x 2^e) and lo = fp16(x 2^e - hi) for re and im,
+// both round-to-nearest, so x 2^e = hi + lo to ~22 significant bits.
+// Output per batch entry: planes [row][k / 16][plane][16] fp16 (re_hi,
+// re_lo, im_hi, im_lo; one 128-byte row per k-step, k zero-padded to a
+// multiple of 16) and the exponents [row] (int).
+__global__ void __launch_bounds__(256) split_fp16_kernel(const float2* __restrict__ src, __half* __restrict__ planes,
+                                                         int* __restrict__ exps, std::uint64_t rows, std::uint64_t k,
+                                                         std::uint64_t kpad, std::uint64_t src_batch_stride) {
+  const std::uint64_t b = blockIdx.y;
+  const float2* sb = src + b * src_batch_stride;
+  __half* pb = planes + b * 4 * rows * kpad;
+  int* eb = exps + b * rows;
+  const int lane = threadIdx.x % 32;
+  const std::uint64_t warps = std::uint64_t(gridDim.x) * (blockDim.x / 32);
+  for (std::uint64_t row = (std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32; row < rows; row += warps) {
+    const float2* r = sb + row * k;
+    float mx = 0.f;
+    for (std::uint64_t kk = lane; kk < k; kk += 32) {
+      const float2 v = r[kk];
+      mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    int e = 0;
+    if (mx > 0.f && isfinite(mx)) {
+      int ex;
+      frexpf(mx, &ex);  // mx in [2^(ex-1), 2^ex)
+      e = 15 - ex;
+    }
+    if (lane == 0) eb[row] = e;
+    __half* out = pb + row * kpad * 4;
+    for (std::uint64_t kk = lane; kk < kpad; kk += 32) {
+      const float2 v = kk < k ? r[kk] : make_float2(0.f, 0.f);
+      const float xr = ldexpf(v.x, e), xi = ldexpf(v.y, e);
+      const __half rh = __float2half_rn(xr), ih = __float2half_rn(xi);
+      __half* o = out + (kk / 16) * 64 + (kk % 16);
+      o[0] = rh;
+      o[16] = __float2half_rn(xr - __half2float(rh));
+      o[32] = ih;
+      o[48] = __float2half_rn(xi - __half2float(ih));
+    }
+  }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static std::once_flag once;
@@ -652,6 +759,25 @@ CUtensorMap plane_map(const float* base, std::uint64_t rows, std::uint64_t kpad,
   return map;
 }
 
+// 4-D map over FP16 planes laid out [batch][rows][kpad / 16][64] (fp16),
+// box {64, 1, box_rows, 1} (one 128-byte row per tile row), 128-byte swizzle.
+CUtensorMap plane_map_f16(const __half* base, std::uint64_t rows, std::uint64_t kpad, int batch, int box_rows) {
+  CUtensorMap map;
+  std::memset(&map, 0, sizeof(map));
+  const std::uint64_t kb = kpad / 16;
+  const cuuint64_t dims[4] = {64, kb, rows, (cuuint64_t)batch};
+  const cuuint64_t strides[3] = {128, kb * 128, rows * kb * 128};
+  const cuuint32_t box[4] = {64, 1, (cuuint32_t)box_rows, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 4, const_cast<__half*>(base), dims, strides, box,
+                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    throw std::string("ERROR (qflex_gb300: tensor cores) --> cuTensorMapEncodeTiled failed: ") +
+        std::to_string((int)r);
+  return map;
+}
+
 void check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw std::string("ERROR (qflex_gb300: CUDA ") + what + ") --> " + cudaGetErrorString(e);
 }
@@ -663,7 +789,11 @@ bool tc_eligible(std::size_t m, std::size_t n, std::size_t k) {
 }
 
 std::size_t tc_workspace_elems(std::size_t m, std::size_t n, std::size_t k) {
-  return 4 * (m + n) * ((k + 7) / 8 * 8);
+  // The larger of the 3xTF32 planes (4 fp32 per element) and the 3xFP16
+  // planes (4 fp16 per element) plus their row exponents.
+  const std::size_t tf32 = 4 * (m + n) * ((k + 7) / 8 * 8);
+  const std::size_t fp16 = 2 * (m + n) * ((k + 15) / 16 * 16) + (m + n);
+  return tf32 > fp16 ? tf32 : fp16;
 }
 
 TcConfig tc_default_config() {
@@ -729,6 +859,38 @@ void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size
   cgemm_tf32x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err,
                                                         chunk, epi_sleep);
   check(cudaGetLastError(), "cgemm_tf32x3");
+}
+
+void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size_t m, std::size_t n,
+                         std::size_t k, std::uint64_t batch_stride, std::uint64_t bt_stride, int batch,
+                         float* workspace, int* err, const TcConfig& cfg, cudaStream_t s) {
+  if (!tc_eligible(m, n, k)) throw std::string("ERROR (qflex_gb300: tensor cores) --> shape not eligible");
+  if (cfg.chunk < 1 || cfg.chunk > 64)
+    throw std::string("ERROR (qflex_gb300: tensor cores) --> chunk length must be 1..64");
+  static std::once_flag attr;
+  std::call_once(attr, [] {
+    check(cudaFuncSetAttribute(cgemm_fp16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
+          "cudaFuncSetAttribute");
+  });
+  const std::size_t kpad = (k + 15) / 16 * 16;
+  __half* pa = reinterpret_cast<__half*>(workspace);
+  __half* pb = pa + 4 * m * kpad * (std::size_t)batch;
+  int* ea = reinterpret_cast<int*>(pb + 4 * n * kpad * (std::size_t)batch);
+  int* eb = ea + m * (std::size_t)batch;
+  {
+    dim3 ga((unsigned)std::min<std::uint64_t>((m + 7) / 8, 152 * 16), (unsigned)batch);
+    split_fp16_kernel<<<ga, 256, 0, s>>>(A, pa, ea, m, k, kpad, batch_stride);
+    dim3 gb((unsigned)std::min<std::uint64_t>((n + 7) / 8, 152 * 16), (unsigned)batch);
+    split_fp16_kernel<<<gb, 256, 0, s>>>(Bt, pb, eb, n, k, kpad, bt_stride);
+    check(cudaGetLastError(), "split_fp16");
+  }
+  const CUtensorMap ma = plane_map_f16(pa, m, kpad, batch, BM);
+  const CUtensorMap mb = plane_map_f16(pb, n, kpad, batch, BN);
+  const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
+  dim3 grid((unsigned)tiles, 1, (unsigned)batch);
+  cgemm_fp16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err,
+                                                        cfg.chunk, 0, ea, eb);
+  check(cudaGetLastError(), "cgemm_fp16x3");
 }
 
 }  // namespace qfx

@@ -31,4 +31,13 @@ void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size
                          std::size_t k, std::uint64_t ac_stride, std::uint64_t bt_stride, int batch,
                          float* workspace, int* err, const TcConfig& cfg, cudaStream_t s);
 
+// The same product with 3xFP16 planes: every row of A and of Bt is scaled by
+// a power of two so that its largest component lies in [2^14, 2^15), split
+// into FP16 hi + lo, multiplied as hi*hi + hi*lo + lo*hi on kind::f16
+// tensor cores (twice the TF32 rate) and unscaled in the epilogue. Always
+// the single-CTA kernel; cfg.variant is ignored.
+void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size_t m, std::size_t n,
+                         std::size_t k, std::uint64_t ac_stride, std::uint64_t bt_stride, int batch,
+                         float* workspace, int* err, const TcConfig& cfg, cudaStream_t s);
+
 }  // namespace qfx

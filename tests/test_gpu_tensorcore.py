@@ -1,4 +1,5 @@
-"""Split-precision (3xTF32) tcgen05 products and the engine in that mode.
+"""Split-precision tcgen05 products (3xTF32, and 3xFP16 with power-of-two
+row scaling) and the engine in those modes; every test runs for both.
 Tolerance: per-amplitude error within 1e-5 of the RMS amplitude against
 the reference's complex<float> results and the FP64 oracle; products within
 2e-5 of the FP64 product relative to its mean magnitude (the FP32
@@ -7,16 +8,16 @@ import numpy as np
 import pytest
 
 from oracle import qflex_oracle as qo
-from qflex_gb300 import TF32X3, Context, rqc
+from qflex_gb300 import FP16X3, TF32X3, Context, rqc
 from tests.conftest import rel_err
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-5
 
 
-@pytest.fixture(scope="module")
-def tc_ctx(built_lib):
-    return Context(0, TF32X3)
+@pytest.fixture(scope="module", params=[TF32X3, FP16X3], ids=["tf32x3", "fp16x3"])
+def tc_ctx(built_lib, request):
+    return Context(0, request.param)
 
 
 # m < 256 runs on the single-CTA kernel, m >= 256 on the CTA-pair kernel;
@@ -108,3 +109,27 @@ def test_tf32x3_vs_fp64_oracle_c1(tc_ctx):
         inp = qo.Input(qo.Circuit.loads(c), qo.load_ordering(o), qo.Grid.loads(g), ini, f)
         want.append(qo.evaluate_circuit(inp, np.complex128)[0][1])
     assert rel_err([a for _, a in out], want) < TOL
+
+
+def test_fp16x3_rows_of_any_magnitude(built_lib):
+    """Rows of A and B spanning 1e-30 .. 1e30: the power-of-two row scales
+    keep every output element within 2e-5 of its own row-column scale."""
+    import torch
+    ctx = Context(0, FP16X3)
+    m, n, k = 256, 128, 64
+    g = np.random.default_rng(3)
+    ra = 10.0 ** g.uniform(-30, 30, size=(m, 1))
+    rb = 10.0 ** g.uniform(-8, 8, size=(1, n))
+    A = ((g.standard_normal((m, k)) + 1j * g.standard_normal((m, k))) * ra).astype(np.complex64)
+    B = ((g.standard_normal((k, n)) + 1j * g.standard_normal((k, n))) * rb).astype(np.complex64)
+    dA, dB = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+    dC = torch.empty((m, n), dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()
+    ctx.multiply(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), m, n, k)
+    ctx.synchronize()
+    got = dC.cpu().numpy().astype(np.complex128)
+    want = A.astype(np.complex128) @ B.astype(np.complex128)
+    scale = ra * rb * np.sqrt(k)  # typical magnitude of each element
+    ok = np.isfinite(scale) & (scale > 1e-36) & (scale < 1e36)  # products FP32 can hold
+    err = np.abs(got - want) / scale
+    assert np.max(err[ok]) < 2e-5, np.max(err[ok])
