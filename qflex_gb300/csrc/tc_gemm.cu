@@ -57,6 +57,7 @@ constexpr int EPI_WARPS = 8;
 constexpr int TMEM_COLS = 4 * BN;         // two chunk buffers of (re, im)
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+static_assert(BM * (BN + 1) * 8 <= STAGES * STAGE_BYTES, "the output tile is staged in the operand stages");
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s per wait
 
 __device__ __forceinline__ std::uint32_t smem_u32(const void* p) {
@@ -340,23 +341,37 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
       __syncwarp();
       if (lane == 0) mbar_arrive(&acc_empty[buf]);
     }
-    if (ok && m0 + row < m) {
-      float2* crow = C + std::uint64_t(batch) * c_batch_stride + std::uint64_t(m0 + row) * n + n0 + half * (BN / 2);
-      const int ncols = n - n0 - half * (BN / 2);
+    // The tile goes out through shared memory so that the global stores
+    // are whole rows: once the last chunk is complete every MMA has read
+    // its operand stages, so they are free. Row stride BN + 1 keeps the
+    // column writes at most 2-way bank conflicted.
+    float2* stile = reinterpret_cast<float2*>(smem);
+    const int ncols = n - n0 - half * (BN / 2);
+    if (ok) {
+      float2* srow = stile + row * (BN + 1) + half * (BN / 2);
       if (KIND == KIND_FP16) {
         // Undo the row scales of A (this row) and B (each column).
-        const int ea = exp_a[std::uint64_t(batch) * m + m0 + row];
+        const int ea = m0 + row < m ? exp_a[std::uint64_t(batch) * m + m0 + row] : 0;
         const int* eb = exp_b + std::uint64_t(batch) * n + n0 + half * (BN / 2);
 #pragma unroll
-        for (int j = 0; j < BN / 2; ++j)
-          if (j < ncols) {
-            const int e = -(ea + eb[j]);
-            crow[j] = make_float2(ldexpf(tre[j], e), ldexpf(tim[j], e));
-          }
+        for (int j = 0; j < BN / 2; ++j) {
+          const int e = j < ncols ? -(ea + eb[j]) : 0;
+          srow[j] = make_float2(ldexpf(tre[j], e), ldexpf(tim[j], e));
+        }
       } else {
 #pragma unroll
-        for (int j = 0; j < BN / 2; ++j)
-          if (j < ncols) crow[j] = make_float2(tre[j], tim[j]);
+        for (int j = 0; j < BN / 2; ++j) srow[j] = make_float2(tre[j], tim[j]);
+      }
+    }
+    asm volatile("bar.sync 1, %0;" ::"r"(32 * EPI_WARPS) : "memory");  // the epilogue warps only
+    if (!*abort_flag) {
+      const int ew = warp - 2;
+      float2* cb = C + std::uint64_t(batch) * c_batch_stride;
+      const int rows = min(BM, m - m0), cols = min(BN, n - n0);
+      for (int r = ew; r < rows; r += EPI_WARPS) {
+        float2* crow = cb + std::uint64_t(m0 + r) * n + n0;
+        const float2* srow = stile + r * (BN + 1);
+        for (int c = lane; c < cols; c += 32) crow[c] = srow[c];
       }
     }
   }
