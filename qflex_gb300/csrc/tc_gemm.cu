@@ -191,7 +191,7 @@ template <int KIND>
 __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const CUtensorMap* map_b,
                                                  float2* __restrict__ C, int m, int n, int k,
                                                  std::uint64_t c_batch_stride, int* __restrict__ err, int CHUNK,
-                                                 int epi_sleep_ns, const int* __restrict__ exp_a,
+                                                 const int* __restrict__ exp_a,
                                                  const int* __restrict__ exp_b) {
   constexpr int KSTEP = KIND == KIND_TF32 ? 8 : 16;  // k values per plane row of 32 bytes
   extern __shared__ __align__(1024) std::uint8_t smem_raw[];
@@ -250,8 +250,8 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
       if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) - 1) & 1, abort_flag, err, 1)) break;
       std::uint8_t* st = smem + s * STAGE_BYTES;
       mbar_expect_tx(&full[s], STAGE_BYTES);
-      tma_load_4d(map_a, &full[s], st, 0, kb, m0, batch);
-      tma_load_4d(map_b, &full[s], st + TILE_A, 0, kb, n0, batch);
+      tma_load_4d(map_a, &full[s], st, 0, m0, kb, batch);
+      tma_load_4d(map_b, &full[s], st + TILE_A, 0, n0, kb, batch);
       issued = kb + 1;
     }
     if (*abort_flag) {
@@ -272,9 +272,15 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
       const int s = kb % STAGES;
       const int c = kb / CHUNK, buf = c & 1;
       const bool first = kb % CHUNK == 0;
-      if (first && c >= 2 && !mbar_wait(&acc_empty[buf], ((c >> 1) - 1) & 1, abort_flag, err, 4)) break;
+      if (first && c >= 2) {
+        // The epilogue's TMEM reads of this buffer precede the MMAs that
+        // overwrite it.
+        if (!mbar_wait(&acc_empty[buf], ((c >> 1) - 1) & 1, abort_flag, err, 4)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+      }
+      // Operand stages need no fence: the TMA's complete_tx on the barrier
+      // orders its shared-memory writes before the MMAs' reads.
       if (!mbar_wait(&full[s], (kb / STAGES) & 1, abort_flag, err, 2)) break;
-      asm volatile("tcgen05.fence::after_thread_sync;");
       const std::uint32_t d_re = tmem + buf * 2 * BN, d_im = d_re + BN;
       const std::uint32_t a0 = smem_u32(smem + s * STAGE_BYTES);
       const std::uint32_t b0 = a0 + TILE_A;
@@ -315,8 +321,6 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     bool ok = true;
     for (int c = 0; c < chunks; ++c) {
       const int buf = c & 1;
-      if (epi_sleep_ns > 0)
-        while (!mbar_test(&acc_full[buf], (c >> 1) & 1) && !*abort_flag) __nanosleep(epi_sleep_ns);
       if (!mbar_wait(&acc_full[buf], (c >> 1) & 1, abort_flag, err, 3)) {
         ok = false;
         break;
@@ -391,16 +395,16 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
 __global__ void __launch_bounds__(THREADS, 1)
     cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                         float2* __restrict__ C, int m, int n, int k, std::uint64_t c_batch_stride,
-                        int* __restrict__ err, int CHUNK, int epi_sleep_ns) {
-  cgemm_split_body<KIND_TF32>(&map_a, &map_b, C, m, n, k, c_batch_stride, err, CHUNK, epi_sleep_ns, nullptr, nullptr);
+                        int* __restrict__ err, int CHUNK) {
+  cgemm_split_body<KIND_TF32>(&map_a, &map_b, C, m, n, k, c_batch_stride, err, CHUNK, nullptr, nullptr);
 }
 
 __global__ void __launch_bounds__(THREADS, 1)
     cgemm_fp16x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                         float2* __restrict__ C, int m, int n, int k, std::uint64_t c_batch_stride,
-                        int* __restrict__ err, int CHUNK, int epi_sleep_ns, const int* __restrict__ exp_a,
+                        int* __restrict__ err, int CHUNK, const int* __restrict__ exp_a,
                         const int* __restrict__ exp_b) {
-  cgemm_split_body<KIND_FP16>(&map_a, &map_b, C, m, n, k, c_batch_stride, err, CHUNK, epi_sleep_ns, exp_a, exp_b);
+  cgemm_split_body<KIND_FP16>(&map_a, &map_b, C, m, n, k, c_batch_stride, err, CHUNK, exp_a, exp_b);
 }
 
 // ---- CTA-pair kernel (cta_group::2) -------------------------------------------
@@ -560,8 +564,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
       std::uint8_t* st = smem + s * P_STAGE_BYTES;
       if (rank == 0) mbar_expect_tx(&full[s], 2 * P_STAGE_BYTES);
       const std::uint32_t bar = peer_addr(&full[s], 0);
-      tma_load_4d_pair(&map_a, bar, st, 0, kb, m0, batch);
-      tma_load_4d_pair(&map_b, bar, st + P_TILE_A, 0, kb, n0 + int(rank) * PBN_CTA, batch);
+      tma_load_4d_pair(&map_a, bar, st, 0, m0, kb, batch);
+      tma_load_4d_pair(&map_b, bar, st + P_TILE_A, 0, n0 + int(rank) * PBN_CTA, kb, batch);
       issued = kb + 1;
     }
     if (*abort_flag && rank == 0) {
@@ -578,9 +582,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
       const int s = kb % P_STAGES;
       const int c = kb / CHUNK, buf = c & 1;
       const bool first = kb % CHUNK == 0;
-      if (first && c >= 2 && !mbar_wait_cluster(&acc_empty[buf], ((c >> 1) - 1) & 1, abort_flag, err, 14)) break;
+      if (first && c >= 2) {
+        if (!mbar_wait_cluster(&acc_empty[buf], ((c >> 1) - 1) & 1, abort_flag, err, 14)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+      }
       if (!mbar_wait_cluster(&full[s], (kb / P_STAGES) & 1, abort_flag, err, 12)) break;
-      asm volatile("tcgen05.fence::after_thread_sync;");
       const std::uint32_t d_re = tmem + buf * 2 * PBN, d_im = d_re + PBN;
       const std::uint32_t a0 = smem_u32(smem + s * P_STAGE_BYTES);
       const std::uint32_t b0 = a0 + P_TILE_A;
@@ -672,8 +678,10 @@ __device__ __forceinline__ float tf32_rn(float x) {
   return __uint_as_float(r);
 }
 
-// Output layout per batch entry: [row][k / 8][plane][8] fp32 with planes
+// Output layout per batch entry: [k / 8][row][plane][8] fp32 with planes
 // re_hi, re_lo, im_hi, im_lo; k is padded to a multiple of 8 with zeros.
+// k-step-major, so the 128 rows of one k-step that a tile loads are one
+// contiguous 16 KB block.
 __global__ void __launch_bounds__(256) split_tf32_kernel(const float2* __restrict__ src, float* __restrict__ planes,
                                                          std::uint64_t rows, std::uint64_t k, std::uint64_t kpad,
                                                          std::uint64_t src_batch_stride) {
@@ -686,7 +694,7 @@ __global__ void __launch_bounds__(256) split_tf32_kernel(const float2* __restric
     const std::uint64_t row = i / kpad, kk = i % kpad;
     const float2 v = kk < k ? sb[row * k + kk] : make_float2(0.f, 0.f);
     const float rh = tf32_rn(v.x), ih = tf32_rn(v.y);
-    float* o = pb + (row * (kpad / 8) + kk / 8) * 32 + (kk % 8);
+    float* o = pb + ((kk / 8) * rows + row) * 32 + (kk % 8);
     o[0] = rh;
     o[8] = tf32_rn(v.x - rh);
     o[16] = ih;
@@ -698,7 +706,7 @@ __global__ void __launch_bounds__(256) split_tf32_kernel(const float2* __restric
 // power-of-two scale e with max * 2^e in [2^14, 2^15) (FP16 holds up to
 // 65504), then hi = fp16(x 2^e) and lo = fp16(x 2^e - hi) for re and im,
 // both round-to-nearest, so x 2^e = hi + lo to ~22 significant bits.
-// Output per batch entry: planes [row][k / 16][plane][16] fp16 (re_hi,
+// Output per batch entry: planes [k / 16][row][plane][16] fp16 (re_hi,
 // re_lo, im_hi, im_lo; one 128-byte row per k-step, k zero-padded to a
 // multiple of 16) and the exponents [row] (int).
 __global__ void __launch_bounds__(256) split_fp16_kernel(const float2* __restrict__ src, __half* __restrict__ planes,
@@ -726,12 +734,11 @@ __global__ void __launch_bounds__(256) split_fp16_kernel(const float2* __restric
       e = 15 - ex;
     }
     if (lane == 0) eb[row] = e;
-    __half* out = pb + row * kpad * 4;
     for (std::uint64_t kk = lane; kk < kpad; kk += 32) {
       const float2 v = kk < k ? r[kk] : make_float2(0.f, 0.f);
       const float xr = ldexpf(v.x, e), xi = ldexpf(v.y, e);
       const __half rh = __float2half_rn(xr), ih = __float2half_rn(xi);
-      __half* o = out + (kk / 16) * 64 + (kk % 16);
+      __half* o = pb + ((kk / 16) * rows + row) * 64 + (kk % 16);
       o[0] = rh;
       o[16] = __float2half_rn(xr - __half2float(rh));
       o[32] = ih;
@@ -755,15 +762,15 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 4-D map over split planes laid out [batch][rows][kpad / 8][32] (fp32),
-// box {32, 1, box_rows, 1} (one 128-byte row per tile row), 128-byte swizzle.
+// 4-D map over split planes laid out [batch][kpad / 8][rows][32] (fp32),
+// box {32, box_rows, 1, 1} (one 128-byte row per tile row), 128-byte swizzle.
 CUtensorMap plane_map(const float* base, std::uint64_t rows, std::uint64_t kpad, int batch, int box_rows) {
   CUtensorMap map;
   std::memset(&map, 0, sizeof(map));
   const std::uint64_t kb = kpad / 8;
-  const cuuint64_t dims[4] = {32, kb, rows, (cuuint64_t)batch};
-  const cuuint64_t strides[3] = {128, kb * 128, rows * kb * 128};
-  const cuuint32_t box[4] = {32, 1, (cuuint32_t)box_rows, 1};
+  const cuuint64_t dims[4] = {32, rows, kb, (cuuint64_t)batch};
+  const cuuint64_t strides[3] = {128, rows * 128, kb * rows * 128};
+  const cuuint32_t box[4] = {32, (cuuint32_t)box_rows, 1, 1};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(base), dims, strides,
                            box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -774,15 +781,15 @@ CUtensorMap plane_map(const float* base, std::uint64_t rows, std::uint64_t kpad,
   return map;
 }
 
-// 4-D map over FP16 planes laid out [batch][rows][kpad / 16][64] (fp16),
-// box {64, 1, box_rows, 1} (one 128-byte row per tile row), 128-byte swizzle.
+// 4-D map over FP16 planes laid out [batch][kpad / 16][rows][64] (fp16),
+// box {64, box_rows, 1, 1} (one 128-byte row per tile row), 128-byte swizzle.
 CUtensorMap plane_map_f16(const __half* base, std::uint64_t rows, std::uint64_t kpad, int batch, int box_rows) {
   CUtensorMap map;
   std::memset(&map, 0, sizeof(map));
   const std::uint64_t kb = kpad / 16;
-  const cuuint64_t dims[4] = {64, kb, rows, (cuuint64_t)batch};
-  const cuuint64_t strides[3] = {128, kb * 128, rows * kb * 128};
-  const cuuint32_t box[4] = {64, 1, (cuuint32_t)box_rows, 1};
+  const cuuint64_t dims[4] = {64, rows, kb, (cuuint64_t)batch};
+  const cuuint64_t strides[3] = {128, rows * 128, kb * rows * 128};
+  const cuuint32_t box[4] = {64, (cuuint32_t)box_rows, 1, 1};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 4, const_cast<__half*>(base), dims, strides, box,
                            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -832,12 +839,6 @@ void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size
   if (cfg.chunk < 1 || cfg.chunk > 64)
     throw std::string("ERROR (qflex_gb300: tensor cores) --> chunk length must be 1..64");
   const int chunk = cfg.chunk;
-  // Epilogue warps of the single-CTA kernel poll the chunk barrier with
-  // this back-off (0: plain bounded wait); QFLEX_TC_EPI_SLEEP_NS overrides.
-  static const int epi_sleep = [] {
-    const char* e = std::getenv("QFLEX_TC_EPI_SLEEP_NS");
-    return e ? std::atoi(e) : 0;
-  }();
   static std::once_flag attr;
   std::call_once(attr, [] {
     check(cudaFuncSetAttribute(cgemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
@@ -872,7 +873,7 @@ void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size
   const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
   dim3 grid((unsigned)tiles, 1, (unsigned)batch);
   cgemm_tf32x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err,
-                                                        chunk, epi_sleep);
+                                                        chunk);
   check(cudaGetLastError(), "cgemm_tf32x3");
 }
 
@@ -904,7 +905,7 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
   const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
   dim3 grid((unsigned)tiles, 1, (unsigned)batch);
   cgemm_fp16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err,
-                                                        cfg.chunk, 0, ea, eb);
+                                                        cfg.chunk, ea, eb);
   check(cudaGetLastError(), "cgemm_fp16x3");
 }
 
