@@ -49,7 +49,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--batch", type=int, default=8, help="output strings per step")
     p.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    p.add_argument("--precision", default="fp16x3", choices=["fp16x3", "tf32x3", "fp32"])
+    p.add_argument("--precision", default="fp16x3", choices=["fp16x3", "tf32x3", "bf16x3", "fp32"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-autotune", action="store_true",
                    help="skip the tensor-core kernel / strings-per-pass autotuning before warm-up")
@@ -314,17 +314,19 @@ def main():
                                "the measured peaks hold no FP32 CUDA-core figure",
                 "traffic": None, "timing": "CUDA events, dominant shape, 5 launches"}
         else:
-            # Split products with 4 real products x 3 terms = 12 MMAs of 2mnk
-            # per 8mnk of algorithmic work. TF32 runs at half the bf16 rate,
-            # FP16 at the bf16 rate.
+            # Split products: 4 real products x 3 terms (3xTF32, 3xFP16) or
+            # x 6 terms (BF16x3) = 12 or 24 MMAs of 2mnk per 8mnk of
+            # algorithmic work. TF32 runs at half the bf16 rate, FP16 and
+            # BF16 at the bf16 rate.
             bf16 = pk.get("bf16_tflops", 1900.0)
-            fp16 = args.precision == "fp16x3"
+            fp16 = args.precision in ("fp16x3", "bf16x3")
             mma_peak = bf16 if fp16 else bf16 / 2
+            terms = 6.0 if args.precision == "bf16x3" else 3.0
             src = "measured bf16 dense burst" if "bf16_tflops" in pk else "fallback 1.9 PFLOP/s bf16"
             line["roofline"] = {
                 "bound": "tensor", "kernel": f"cgemm_{args.precision} ({m},{n},{k}) incl. plane splits",
-                "achieved": 3.0 * achieved, "achieved_algorithmic": achieved, "peak": mma_peak,
-                "unit": "TFLOP/s (FP16 MMA)" if fp16 else "TFLOP/s (TF32 MMA)", "frac": 3.0 * achieved / mma_peak,
+                "achieved": terms * achieved, "achieved_algorithmic": achieved, "peak": mma_peak,
+                "unit": "TFLOP/s (16-bit MMA)" if fp16 else "TFLOP/s (TF32 MMA)", "frac": terms * achieved / mma_peak,
                 "peak_source": src + (" (MEASURED_PEAKS.json)" if "bf16_tflops" in pk else "") + ("" if fp16 else " / 2"),
                 "traffic": TRAFFIC.get((args.precision, m, n, k)),
                 "traffic_source": "ncu dram__bytes_read+write of one launch of this shape (profiles/)",
@@ -332,7 +334,7 @@ def main():
             # The other paths on the same workload, one step each (after a
             # warm-up step): the plain FP32 CUDA-core path the metric compares
             # against, and the other split-precision mode.
-            for other in [q for q in ("fp32", "tf32x3", "fp16x3") if q != args.precision]:
+            for other in [q for q in ("fp32", "tf32x3", "bf16x3", "fp16x3") if q != args.precision]:
                 fp = Context(local)
                 fp.set_precision(other)
                 fp.set_stream(stream.cuda_stream)

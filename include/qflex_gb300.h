@@ -31,7 +31,7 @@ extern "C" {
 /* Arithmetic of the complex64 contractions. */
 #define QFLEX_GB300_FP32 0   /* FP32 CUDA cores (matches complex<float>) */
 #define QFLEX_GB300_TF32X3 1 /* split 3xTF32 on tcgen05 tensor cores */
-#define QFLEX_GB300_BF16X3 2 /* split BF16x3 on tcgen05 tensor cores (not available) */
+#define QFLEX_GB300_BF16X3 2 /* split BF16x3 (six products per real product) on tcgen05 tensor cores */
 #define QFLEX_GB300_FP16X3 3 /* split 3xFP16 (rows scaled by powers of two) on tcgen05 tensor cores */
 
 typedef struct qflex_gb300_context qflex_gb300_context;

@@ -4,7 +4,7 @@
 //
 //   qflex <circuit> <ordering> <grid> [<initial_conf> <final_conf> <verbosity> <memory_limit>]
 //   qflex -c <circuit> -o <ordering> -g <grid> [--initial-conf=S] [--final-conf=S]
-//         [--verbosity=N] [--memory=M] [--device=N] [--precision=fp32|tf32x3|fp16x3]
+//         [--verbosity=N] [--memory=M] [--device=N] [--precision=fp32|tf32x3|fp16x3|bf16x3]
 //
 // Output: one line "<initial> --> <state>: <re> <im>" per amplitude.
 // Exit codes: 0 ok, 1 std::exception, 2 error message (thrown string).
@@ -42,7 +42,7 @@ const char* kUsage =
     "  qflex <circuit_filename> <ordering_filename> <grid_filename> [<initial_conf> <final_conf> "
     "<verbosity_level> <memory_limit>]\n"
     "  qflex -c <circuit_filename> -o <ordering_filename> -g <grid_filename> [--initial-conf=S "
-    "--final-conf=S --verbosity=N --memory=M --device=N --precision=fp32|tf32x3|fp16x3]\n";
+    "--final-conf=S --verbosity=N --memory=M --device=N --precision=fp32|tf32x3|fp16x3|bf16x3]\n";
 
 }  // namespace
 
@@ -91,6 +91,8 @@ int main(int argc, char** argv) {
         qflex::global::precision = QFLEX_GB300_TF32X3;
       else if (p == "fp16x3")
         qflex::global::precision = QFLEX_GB300_FP16X3;
+      else if (p == "bf16x3")
+        qflex::global::precision = QFLEX_GB300_BF16X3;
       else
         throw std::string("Unknown precision ") + p;
     }

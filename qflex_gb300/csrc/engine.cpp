@@ -102,7 +102,8 @@ Engine::~Engine() {
 }
 
 void Engine::set_precision(int p) {
-  if (p != FP32 && p != TF32X3 && p != FP16X3) throw QFX_ERR("Precision mode ", p, " is not available in this build.");
+  if (p != FP32 && p != TF32X3 && p != FP16X3 && p != BF16X3)
+    throw QFX_ERR("Precision mode ", p, " is not available in this build.");
   precision_ = p;
 }
 
@@ -144,6 +145,18 @@ void Engine::set_tc_variant(std::size_t m, std::size_t n, std::size_t k, int var
   ++options_version_;
 }
 
+void Engine::launch_split_product(const float2* A, const float2* Bt, float2* C, std::size_t m, std::size_t n,
+                                  std::size_t k, std::uint64_t ac_stride, std::uint64_t bt_stride, int batch,
+                                  float* ws) {
+  const TcConfig cfg = tc_config(m, n, k);
+  if (precision_ == FP16X3)
+    launch_cgemm_fp16x3(A, Bt, C, m, n, k, ac_stride, bt_stride, batch, ws, error_flag(), cfg, stream_);
+  else if (precision_ == BF16X3)
+    launch_cgemm_bf16x3(A, Bt, C, m, n, k, ac_stride, bt_stride, batch, ws, error_flag(), cfg, stream_);
+  else
+    launch_cgemm_tf32x3(A, Bt, C, m, n, k, ac_stride, bt_stride, batch, ws, error_flag(), cfg, stream_);
+}
+
 TcConfig Engine::tc_config(std::size_t m, std::size_t n, std::size_t k) const {
   TcConfig c = tc_cfg_;
   const auto it = tc_variant_.find({m, n, k});
@@ -169,7 +182,7 @@ void Engine::check_error_flag() {
 
 void Engine::multiply(const float2* A, const float2* B, float2* C, std::size_t m, std::size_t n,
                       std::size_t k, std::uint64_t stride, int batch) {
-  if ((precision_ == TF32X3 || precision_ == FP16X3) && tc_eligible(m, n, k)) {
+  if (precision_ != FP32 && tc_eligible(m, n, k)) {
     // The tensor-core kernel reads B as [n][k]: transpose into the front of
     // the workspace, split planes after it.
     const std::size_t bt = ((n * k * (std::size_t)batch + 63) / 64) * 64;
@@ -188,12 +201,7 @@ void Engine::multiply(const float2* A, const float2* B, float2* C, std::size_t m
       make_perm_plan(nbits, perm, &plan);
       for (int b = 0; b < batch; ++b)
         launch_permute(plan, B + (std::size_t)b * stride, Bt + (std::size_t)b * n * k, 0, 1, stream_);
-      if (precision_ == FP16X3)
-        launch_cgemm_fp16x3(A, Bt, C, m, n, k, stride, n * k, batch, ws + 2 * bt, error_flag(),
-                            tc_config(m, n, k), stream_);
-      else
-        launch_cgemm_tf32x3(A, Bt, C, m, n, k, stride, n * k, batch, ws + 2 * bt, error_flag(),
-                            tc_config(m, n, k), stream_);
+      launch_split_product(A, Bt, C, m, n, k, stride, n * k, batch, ws + 2 * bt);
       return;
     }
   }
@@ -344,12 +352,8 @@ std::size_t Engine::run_program(Plan& p, int batch, float2* arena, float* tc_ws)
       launch_permute(p.perm[i], arena + op.a, arena + op.c, stride, batch, stream_);
       launches += 1;
     } else if (op.b_nk) {
-      if (precision_ == FP16X3)
-        launch_cgemm_fp16x3(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, stride,
-                            batch, tc_ws, err, tc_config(op.m, op.n, op.k), stream_);
-      else
-        launch_cgemm_tf32x3(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, stride,
-                            batch, tc_ws, err, tc_config(op.m, op.n, op.k), stream_);
+      launch_split_product(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, stride, batch,
+                           tc_ws);
       launches += 3;  // two plane splits and the product
     } else {
       launch_cgemm_fp32(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, batch,
@@ -421,7 +425,7 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
   if (!p.built) {
     p.net = build_network(p.circuit, p.grid, initial, results[0].final_state, final_qubits, p.ops);
     std::function<bool(std::size_t, std::size_t, std::size_t)> b_kmajor;
-    if (precision_ == TF32X3 || precision_ == FP16X3) b_kmajor = tc_eligible;
+    if (precision_ != FP32) b_kmajor = tc_eligible;
     try {
       p.prog = plan_contraction(p.net, p.ops, results[0].states.size(), INFINITY, b_kmajor);
     } catch (const std::string& e) {

@@ -116,6 +116,9 @@ class Engine {
   int max_batch_ = 0;            // output strings per device pass (0: as many as fit)
   unsigned options_version_ = 0;  // part of the graph key: options change launches
   TcConfig tc_config(std::size_t m, std::size_t n, std::size_t k) const;
+  // C = A * Bt^T on the tensor cores in the context's split precision.
+  void launch_split_product(const float2* A, const float2* Bt, float2* C, std::size_t m, std::size_t n,
+                            std::size_t k, std::uint64_t ac_stride, std::uint64_t bt_stride, int batch, float* ws);
   std::vector<cudaEvent_t> prof_events_;
   std::vector<double> op_ms_;
   std::unique_ptr<Plan> plan_;

@@ -32,6 +32,7 @@
 // frees its TMEM before returning.
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include <cstdlib>
@@ -123,6 +124,18 @@ __device__ __forceinline__ std::uint64_t smem_desc_sw128(std::uint32_t addr) {
   return d;
 }
 
+// The same for rows of 64 bytes in the 64-byte swizzle (8-row groups 512
+// bytes apart); the BF16x3 kernel keeps its third pieces there.
+__device__ __forceinline__ std::uint64_t smem_desc_sw64(std::uint32_t addr) {
+  std::uint64_t d = 0;
+  d |= std::uint64_t((addr & 0x3FFFF) >> 4);
+  d |= std::uint64_t(1) << 16;
+  d |= std::uint64_t(512 >> 4) << 32;
+  d |= std::uint64_t(1) << 46;
+  d |= std::uint64_t(4) << 61;                     // 64-byte swizzle
+  return d;
+}
+
 // Instruction descriptor, kind::tf32: D = F32, A = B = TF32, both K-major.
 __host__ __device__ constexpr std::uint32_t idesc_tf32(int m, int n, bool negate_a) {
   return (1u << 4) | (2u << 7) | (2u << 10) | (negate_a ? (1u << 13) : 0u) |
@@ -150,7 +163,8 @@ __device__ __forceinline__ void umma_f16(std::uint32_t d_tmem, std::uint64_t a, 
 // Operand kinds of the single-CTA kernel: 3xTF32 planes (8 values of 4
 // bytes per plane and k-step) or 3xFP16 planes (16 values of 2 bytes, rows
 // scaled by powers of two).
-enum SplitKind : int { KIND_TF32 = 0, KIND_FP16 = 1 };
+// BF16x3: three BF16 pieces per value (x = b0 + b1 + b2 to ~24 bits).
+enum SplitKind : int { KIND_TF32 = 0, KIND_FP16 = 1, KIND_BF16 = 2 };
 template <int KIND>
 __device__ __forceinline__ void umma(std::uint32_t d, std::uint64_t a, std::uint64_t b, std::uint32_t id,
                                      std::uint32_t acc) {
@@ -159,9 +173,14 @@ __device__ __forceinline__ void umma(std::uint32_t d, std::uint64_t a, std::uint
   else
     umma_f16(d, a, b, id, acc);
 }
+// kind::f16 with BF16 A and B (format 1), F32 D.
+__host__ __device__ constexpr std::uint32_t idesc_bf16(int m, int n, bool negate_a) {
+  return idesc_f16(m, n, negate_a) | (1u << 7) | (1u << 10);
+}
 template <int KIND>
 __host__ __device__ constexpr std::uint32_t idesc_kind(int m, int n, bool negate_a) {
-  return KIND == KIND_TF32 ? idesc_tf32(m, n, negate_a) : idesc_f16(m, n, negate_a);
+  return KIND == KIND_TF32 ? idesc_tf32(m, n, negate_a)
+                           : (KIND == KIND_FP16 ? idesc_f16(m, n, negate_a) : idesc_bf16(m, n, negate_a));
 }
 
 __device__ __forceinline__ void umma_commit(std::uint64_t* bar) {
@@ -187,19 +206,28 @@ __device__ __forceinline__ void mbar_arrive(std::uint64_t* bar) {
 
 // The single-CTA kernel body. KIND_FP16 operands carry per-row scale
 // exponents (value = plane value * 2^-e); the epilogue removes them.
+// KIND_BF16 operands have six planes per k-step: b0, b1 of re and im in a
+// 128-byte row (map_a / map_b) and b2 of re and im in a 64-byte row
+// (map_a2 / map_b2); its stages are 48 KB, four of them.
 template <int KIND>
 __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const CUtensorMap* map_b,
+                                                 const CUtensorMap* map_a2, const CUtensorMap* map_b2,
                                                  float2* __restrict__ C, int m, int n, int k,
                                                  std::uint64_t c_batch_stride, int* __restrict__ err, int CHUNK,
                                                  const int* __restrict__ exp_a,
                                                  const int* __restrict__ exp_b) {
   constexpr int KSTEP = KIND == KIND_TF32 ? 8 : 16;  // k values per plane row of 32 bytes
+  constexpr int TAIL = BM * 64;                       // BF16 third-piece tile of one operand
+  constexpr int NST = KIND == KIND_BF16 ? 4 : STAGES;
+  constexpr int SBYTES = KIND == KIND_BF16 ? 2 * (TILE_A + TAIL) : STAGE_BYTES;
+  static_assert(NST * SBYTES <= STAGES * STAGE_BYTES, "stages fit the shared memory of the launch");
+  static_assert(BM * (BN + 1) * 8 <= NST * SBYTES, "the output tile is staged in the operand stages");
   extern __shared__ __align__(1024) std::uint8_t smem_raw[];
   std::uint8_t* smem = reinterpret_cast<std::uint8_t*>((reinterpret_cast<std::uintptr_t>(smem_raw) + 1023) &
                                                        ~std::uintptr_t(1023));
-  std::uint64_t* full = reinterpret_cast<std::uint64_t*>(smem + STAGES * STAGE_BYTES);
-  std::uint64_t* empty = full + STAGES;
-  std::uint64_t* acc_full = empty + STAGES;   // [2]: a chunk accumulator is complete
+  std::uint64_t* full = reinterpret_cast<std::uint64_t*>(smem + NST * SBYTES);
+  std::uint64_t* empty = full + NST;
+  std::uint64_t* acc_full = empty + NST;   // [2]: a chunk accumulator is complete
   std::uint64_t* acc_empty = acc_full + 2;    // [2]: a chunk accumulator was drained
   std::uint64_t* mma_done = acc_empty + 2;    // every issued MMA has completed
   std::uint32_t* tmem_slot = reinterpret_cast<std::uint32_t*>(mma_done + 1);
@@ -220,7 +248,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
   const int chunks = (kblocks + CHUNK - 1) / CHUNK;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; ++s) {
+    for (int s = 0; s < NST; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
@@ -246,20 +274,24 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     // Producer.
     int issued = 0;
     for (int kb = 0; kb < kblocks; ++kb) {
-      const int s = kb % STAGES;
-      if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) - 1) & 1, abort_flag, err, 1)) break;
-      std::uint8_t* st = smem + s * STAGE_BYTES;
-      mbar_expect_tx(&full[s], STAGE_BYTES);
+      const int s = kb % NST;
+      if (kb >= NST && !mbar_wait(&empty[s], ((kb / NST) - 1) & 1, abort_flag, err, 1)) break;
+      std::uint8_t* st = smem + s * SBYTES;
+      mbar_expect_tx(&full[s], SBYTES);
       tma_load_4d(map_a, &full[s], st, 0, m0, kb, batch);
       tma_load_4d(map_b, &full[s], st + TILE_A, 0, n0, kb, batch);
+      if constexpr (KIND == KIND_BF16) {
+        tma_load_4d(map_a2, &full[s], st + 2 * TILE_A, 0, m0, kb, batch);
+        tma_load_4d(map_b2, &full[s], st + 2 * TILE_A + TAIL, 0, n0, kb, batch);
+      }
       issued = kb + 1;
     }
     if (*abort_flag) {
       // Let the copies already issued land before the CTA's shared memory
       // is released (bounded as well).
-      for (int kb = issued > STAGES ? issued - STAGES : 0; kb < issued; ++kb) {
+      for (int kb = issued > NST ? issued - NST : 0; kb < issued; ++kb) {
         const unsigned long long t0 = now_ns();
-        while (!mbar_test(&full[kb % STAGES], (kb / STAGES) & 1) && now_ns() - t0 < WAIT_NS) {
+        while (!mbar_test(&full[kb % NST], (kb / NST) & 1) && now_ns() - t0 < WAIT_NS) {
         }
       }
     }
@@ -269,7 +301,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     // the epilogue warps add it into their FP32 registers and free it.
     const std::uint32_t idp = idesc_kind<KIND>(BM, BN, false), idn = idesc_kind<KIND>(BM, BN, true);
     for (int kb = 0; kb < kblocks; ++kb) {
-      const int s = kb % STAGES;
+      const int s = kb % NST;
       const int c = kb / CHUNK, buf = c & 1;
       const bool first = kb % CHUNK == 0;
       if (first && c >= 2) {
@@ -280,17 +312,55 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
       }
       // Operand stages need no fence: the TMA's complete_tx on the barrier
       // orders its shared-memory writes before the MMAs' reads.
-      if (!mbar_wait(&full[s], (kb / STAGES) & 1, abort_flag, err, 2)) break;
+      if (!mbar_wait(&full[s], (kb / NST) & 1, abort_flag, err, 2)) break;
       const std::uint32_t d_re = tmem + buf * 2 * BN, d_im = d_re + BN;
-      const std::uint32_t a0 = smem_u32(smem + s * STAGE_BYTES);
+      const std::uint32_t a0 = smem_u32(smem + s * SBYTES);
       const std::uint32_t b0 = a0 + TILE_A;
       const std::uint64_t arh = smem_desc_sw128(a0), arl = smem_desc_sw128(a0 + 32),
                           aih = smem_desc_sw128(a0 + 64), ail = smem_desc_sw128(a0 + 96);
       const std::uint64_t brh = smem_desc_sw128(b0), brl = smem_desc_sw128(b0 + 32),
                           bih = smem_desc_sw128(b0 + 64), bil = smem_desc_sw128(b0 + 96);
+      const std::uint32_t acc = first ? 0u : 1u;
+      if constexpr (KIND == KIND_BF16) {
+        // Pieces 0 and 1 sit in the 128-byte rows (re0 re1 im0 im1, named
+        // *h and *l above), piece 2 in the 64-byte rows (re2 im2). Per real
+        // product x*y the terms x2y0, x1y1, x0y2 (~2^-16), x1y0, x0y1
+        // (~2^-8) and x0y0, smallest first.
+        const std::uint32_t at = a0 + 2 * TILE_A, bt = at + TAIL;
+        const std::uint64_t ar2 = smem_desc_sw64(at), ai2 = smem_desc_sw64(at + 32);
+        const std::uint64_t br2 = smem_desc_sw64(bt), bi2 = smem_desc_sw64(bt + 32);
+        // C_re = Ar Br - Ai Bi
+        umma<KIND>(d_re, ar2, brh, idp, acc);
+        umma<KIND>(d_re, arl, brl, idp, 1);
+        umma<KIND>(d_re, arh, br2, idp, 1);
+        umma<KIND>(d_re, ai2, bih, idn, 1);
+        umma<KIND>(d_re, ail, bil, idn, 1);
+        umma<KIND>(d_re, aih, bi2, idn, 1);
+        umma<KIND>(d_re, arl, brh, idp, 1);
+        umma<KIND>(d_re, arh, brl, idp, 1);
+        umma<KIND>(d_re, ail, bih, idn, 1);
+        umma<KIND>(d_re, aih, bil, idn, 1);
+        umma<KIND>(d_re, arh, brh, idp, 1);
+        umma<KIND>(d_re, aih, bih, idn, 1);
+        // C_im = Ar Bi + Ai Br
+        umma<KIND>(d_im, ar2, bih, idp, acc);
+        umma<KIND>(d_im, arl, bil, idp, 1);
+        umma<KIND>(d_im, arh, bi2, idp, 1);
+        umma<KIND>(d_im, ai2, brh, idp, 1);
+        umma<KIND>(d_im, ail, brl, idp, 1);
+        umma<KIND>(d_im, aih, br2, idp, 1);
+        umma<KIND>(d_im, arl, bih, idp, 1);
+        umma<KIND>(d_im, arh, bil, idp, 1);
+        umma<KIND>(d_im, ail, brh, idp, 1);
+        umma<KIND>(d_im, aih, brl, idp, 1);
+        umma<KIND>(d_im, arh, bih, idp, 1);
+        umma<KIND>(d_im, aih, brh, idp, 1);
+        umma_commit(&empty[s]);
+        if (kb % CHUNK == CHUNK - 1 || kb == kblocks - 1) umma_commit(&acc_full[buf]);
+        continue;
+      }
       // The small hi*lo terms go first and the two large hi*hi terms last,
       // so only those two additions round against a large accumulator.
-      const std::uint32_t acc = first ? 0u : 1u;
       umma<KIND>(d_re, arh, brl, idp, acc);
       umma<KIND>(d_re, arl, brh, idp, 1);
       umma<KIND>(d_re, aih, bil, idn, 1);
@@ -396,7 +466,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                         float2* __restrict__ C, int m, int n, int k, std::uint64_t c_batch_stride,
                         int* __restrict__ err, int CHUNK) {
-  cgemm_split_body<KIND_TF32>(&map_a, &map_b, C, m, n, k, c_batch_stride, err, CHUNK, nullptr, nullptr);
+  cgemm_split_body<KIND_TF32>(&map_a, &map_b, nullptr, nullptr, C, m, n, k, c_batch_stride, err, CHUNK, nullptr,
+                              nullptr);
 }
 
 __global__ void __launch_bounds__(THREADS, 1)
@@ -404,7 +475,17 @@ __global__ void __launch_bounds__(THREADS, 1)
                         float2* __restrict__ C, int m, int n, int k, std::uint64_t c_batch_stride,
                         int* __restrict__ err, int CHUNK, const int* __restrict__ exp_a,
                         const int* __restrict__ exp_b) {
-  cgemm_split_body<KIND_FP16>(&map_a, &map_b, C, m, n, k, c_batch_stride, err, CHUNK, exp_a, exp_b);
+  cgemm_split_body<KIND_FP16>(&map_a, &map_b, nullptr, nullptr, C, m, n, k, c_batch_stride, err, CHUNK, exp_a,
+                              exp_b);
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    cgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                        const __grid_constant__ CUtensorMap map_a2, const __grid_constant__ CUtensorMap map_b2,
+                        float2* __restrict__ C, int m, int n, int k, std::uint64_t c_batch_stride,
+                        int* __restrict__ err, int CHUNK) {
+  cgemm_split_body<KIND_BF16>(&map_a, &map_b, &map_a2, &map_b2, C, m, n, k, c_batch_stride, err, CHUNK, nullptr,
+                              nullptr);
 }
 
 // ---- CTA-pair kernel (cta_group::2) -------------------------------------------
@@ -678,27 +759,55 @@ __device__ __forceinline__ float tf32_rn(float x) {
   return __uint_as_float(r);
 }
 
+// Row access shared by the split kernels: one warp per row, lanes over k.
+// A row whose start is 16-byte aligned (and k even) is read as float4 pairs.
+struct RowReader {
+  const float2* r;
+  std::uint64_t k;
+  bool vec;
+  __device__ RowReader(const float2* row, std::uint64_t k_)
+      : r(row), k(k_), vec(((reinterpret_cast<std::uintptr_t>(row) & 15) == 0) && (k_ % 2 == 0)) {}
+  // Values kk and kk + 1 (kk even), zero beyond k.
+  __device__ __forceinline__ void pair(std::uint64_t kk, float2& v0, float2& v1) const {
+    if (kk >= k) {
+      v0 = v1 = make_float2(0.f, 0.f);
+    } else if (vec) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(r + kk));
+      v0 = make_float2(v.x, v.y);
+      v1 = make_float2(v.z, v.w);
+    } else {
+      v0 = r[kk];
+      v1 = kk + 1 < k ? r[kk + 1] : make_float2(0.f, 0.f);
+    }
+  }
+};
+
 // Output layout per batch entry: [k / 8][row][plane][8] fp32 with planes
 // re_hi, re_lo, im_hi, im_lo; k is padded to a multiple of 8 with zeros.
 // k-step-major, so the 128 rows of one k-step that a tile loads are one
-// contiguous 16 KB block.
+// contiguous 16 KB block. One warp per row; lane j covers k = 2j, 2j + 1 of
+// every 64.
 __global__ void __launch_bounds__(256) split_tf32_kernel(const float2* __restrict__ src, float* __restrict__ planes,
                                                          std::uint64_t rows, std::uint64_t k, std::uint64_t kpad,
                                                          std::uint64_t src_batch_stride) {
   const std::uint64_t b = blockIdx.y;
   const float2* sb = src + b * src_batch_stride;
   float* pb = planes + b * 4 * rows * kpad;
-  const std::uint64_t count = rows * kpad;
-  for (std::uint64_t i = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count;
-       i += std::uint64_t(gridDim.x) * blockDim.x) {
-    const std::uint64_t row = i / kpad, kk = i % kpad;
-    const float2 v = kk < k ? sb[row * k + kk] : make_float2(0.f, 0.f);
-    const float rh = tf32_rn(v.x), ih = tf32_rn(v.y);
-    float* o = pb + ((kk / 8) * rows + row) * 32 + (kk % 8);
-    o[0] = rh;
-    o[8] = tf32_rn(v.x - rh);
-    o[16] = ih;
-    o[24] = tf32_rn(v.y - ih);
+  const int lane = threadIdx.x % 32;
+  const std::uint64_t warps = std::uint64_t(gridDim.x) * (blockDim.x / 32);
+  for (std::uint64_t row = (std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32; row < rows; row += warps) {
+    const RowReader rd(sb + row * k, k);
+#pragma unroll 4
+    for (std::uint64_t kk = 2 * lane; kk < kpad; kk += 64) {
+      float2 v0, v1;
+      rd.pair(kk, v0, v1);
+      const float rh0 = tf32_rn(v0.x), ih0 = tf32_rn(v0.y), rh1 = tf32_rn(v1.x), ih1 = tf32_rn(v1.y);
+      float* o = pb + ((kk / 8) * rows + row) * 32 + (kk % 8);
+      *reinterpret_cast<float2*>(o) = make_float2(rh0, rh1);
+      *reinterpret_cast<float2*>(o + 8) = make_float2(tf32_rn(v0.x - rh0), tf32_rn(v1.x - rh1));
+      *reinterpret_cast<float2*>(o + 16) = make_float2(ih0, ih1);
+      *reinterpret_cast<float2*>(o + 24) = make_float2(tf32_rn(v0.y - ih0), tf32_rn(v1.y - ih1));
+    }
   }
 }
 
@@ -719,11 +828,13 @@ __global__ void __launch_bounds__(256) split_fp16_kernel(const float2* __restric
   const int lane = threadIdx.x % 32;
   const std::uint64_t warps = std::uint64_t(gridDim.x) * (blockDim.x / 32);
   for (std::uint64_t row = (std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32; row < rows; row += warps) {
-    const float2* r = sb + row * k;
+    const RowReader rd(sb + row * k, k);
     float mx = 0.f;
-    for (std::uint64_t kk = lane; kk < k; kk += 32) {
-      const float2 v = r[kk];
-      mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+#pragma unroll 4
+    for (std::uint64_t kk = 2 * lane; kk < k; kk += 64) {
+      float2 v0, v1;
+      rd.pair(kk, v0, v1);
+      mx = fmaxf(mx, fmaxf(fmaxf(fabsf(v0.x), fabsf(v0.y)), fmaxf(fabsf(v1.x), fabsf(v1.y))));
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -734,15 +845,61 @@ __global__ void __launch_bounds__(256) split_fp16_kernel(const float2* __restric
       e = 15 - ex;
     }
     if (lane == 0) eb[row] = e;
-    for (std::uint64_t kk = lane; kk < kpad; kk += 32) {
-      const float2 v = kk < k ? r[kk] : make_float2(0.f, 0.f);
-      const float xr = ldexpf(v.x, e), xi = ldexpf(v.y, e);
-      const __half rh = __float2half_rn(xr), ih = __float2half_rn(xi);
+#pragma unroll 4
+    for (std::uint64_t kk = 2 * lane; kk < kpad; kk += 64) {
+      float2 v0, v1;
+      rd.pair(kk, v0, v1);
+      const float r0 = ldexpf(v0.x, e), i0 = ldexpf(v0.y, e), r1 = ldexpf(v1.x, e), i1 = ldexpf(v1.y, e);
+      const __half2 rh = __floats2half2_rn(r0, r1), ih = __floats2half2_rn(i0, i1);
+      const float2 rhf = __half22float2(rh), ihf = __half22float2(ih);
       __half* o = pb + ((kk / 16) * rows + row) * 64 + (kk % 16);
-      o[0] = rh;
-      o[16] = __float2half_rn(xr - __half2float(rh));
-      o[32] = ih;
-      o[48] = __float2half_rn(xi - __half2float(ih));
+      *reinterpret_cast<__half2*>(o) = rh;
+      *reinterpret_cast<__half2*>(o + 16) = __floats2half2_rn(r0 - rhf.x, r1 - rhf.y);
+      *reinterpret_cast<__half2*>(o + 32) = ih;
+      *reinterpret_cast<__half2*>(o + 48) = __floats2half2_rn(i0 - ihf.x, i1 - ihf.y);
+    }
+  }
+}
+
+// BF16x3 planes: x = b0 + b1 + b2 with b0 = bf16(x), b1 = bf16(x - b0),
+// b2 = bf16(x - b0 - b1), all round-to-nearest. Output per batch entry:
+// main planes [k / 16][row][64] bf16 (re0, re1, im0, im1; 128 bytes per
+// k-step) and tail planes [k / 16][row][32] bf16 (re2, im2; 64 bytes), k
+// zero-padded to a multiple of 16.
+__global__ void __launch_bounds__(256) split_bf16_kernel(const float2* __restrict__ src,
+                                                         __nv_bfloat16* __restrict__ main_planes,
+                                                         __nv_bfloat16* __restrict__ tail_planes, std::uint64_t rows,
+                                                         std::uint64_t k, std::uint64_t kpad,
+                                                         std::uint64_t src_batch_stride) {
+  const std::uint64_t b = blockIdx.y;
+  const float2* sb = src + b * src_batch_stride;
+  __nv_bfloat16* mb = main_planes + b * 4 * rows * kpad;
+  __nv_bfloat16* tb = tail_planes + b * 2 * rows * kpad;
+  const int lane = threadIdx.x % 32;
+  const std::uint64_t warps = std::uint64_t(gridDim.x) * (blockDim.x / 32);
+  for (std::uint64_t row = (std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) / 32; row < rows; row += warps) {
+    const RowReader rd(sb + row * k, k);
+#pragma unroll 4
+    for (std::uint64_t kk = 2 * lane; kk < kpad; kk += 64) {
+      float2 v0, v1;
+      rd.pair(kk, v0, v1);
+      // Pieces of (re, im) of values kk and kk + 1, two at a time.
+      const __nv_bfloat162 r0 = __floats2bfloat162_rn(v0.x, v1.x), i0 = __floats2bfloat162_rn(v0.y, v1.y);
+      const float2 r0f = __bfloat1622float2(r0), i0f = __bfloat1622float2(i0);
+      const float2 rr = make_float2(v0.x - r0f.x, v1.x - r0f.y), ir = make_float2(v0.y - i0f.x, v1.y - i0f.y);
+      const __nv_bfloat162 r1 = __floats2bfloat162_rn(rr.x, rr.y), i1 = __floats2bfloat162_rn(ir.x, ir.y);
+      const float2 r1f = __bfloat1622float2(r1), i1f = __bfloat1622float2(i1);
+      const __nv_bfloat162 r2 = __floats2bfloat162_rn(rr.x - r1f.x, rr.y - r1f.y);
+      const __nv_bfloat162 i2 = __floats2bfloat162_rn(ir.x - i1f.x, ir.y - i1f.y);
+      const std::uint64_t slot = (kk / 16) * rows + row;
+      __nv_bfloat16* m = mb + slot * 64 + (kk % 16);
+      *reinterpret_cast<__nv_bfloat162*>(m) = r0;
+      *reinterpret_cast<__nv_bfloat162*>(m + 16) = r1;
+      *reinterpret_cast<__nv_bfloat162*>(m + 32) = i0;
+      *reinterpret_cast<__nv_bfloat162*>(m + 48) = i1;
+      __nv_bfloat16* t = tb + slot * 32 + (kk % 16);
+      *reinterpret_cast<__nv_bfloat162*>(t) = r2;
+      *reinterpret_cast<__nv_bfloat162*>(t + 16) = i2;
     }
   }
 }
@@ -800,6 +957,28 @@ CUtensorMap plane_map_f16(const __half* base, std::uint64_t rows, std::uint64_t 
   return map;
 }
 
+// 4-D map over BF16 planes laid out [batch][kpad / 16][rows][inner] with
+// `inner` 64 (128-byte rows, 128-byte swizzle) or 32 (64-byte rows, 64-byte
+// swizzle); box {inner, box_rows, 1, 1}.
+CUtensorMap plane_map_bf16(const __nv_bfloat16* base, std::uint64_t rows, std::uint64_t kpad, int batch,
+                           int box_rows, int inner) {
+  CUtensorMap map;
+  std::memset(&map, 0, sizeof(map));
+  const std::uint64_t kb = kpad / 16, rb = std::uint64_t(inner) * 2;
+  const cuuint64_t dims[4] = {(cuuint64_t)inner, rows, kb, (cuuint64_t)batch};
+  const cuuint64_t strides[3] = {rb, rows * rb, kb * rows * rb};
+  const cuuint32_t box[4] = {(cuuint32_t)inner, (cuuint32_t)box_rows, 1, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(base), dims,
+                           strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           inner == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    throw std::string("ERROR (qflex_gb300: tensor cores) --> cuTensorMapEncodeTiled failed: ") +
+        std::to_string((int)r);
+  return map;
+}
+
 void check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw std::string("ERROR (qflex_gb300: CUDA ") + what + ") --> " + cudaGetErrorString(e);
 }
@@ -811,8 +990,9 @@ bool tc_eligible(std::size_t m, std::size_t n, std::size_t k) {
 }
 
 std::size_t tc_workspace_elems(std::size_t m, std::size_t n, std::size_t k) {
-  // The larger of the 3xTF32 planes (4 fp32 per element) and the 3xFP16
-  // planes (4 fp16 per element) plus their row exponents.
+  // The largest of the 3xTF32 planes (4 fp32 per element), the 3xFP16
+  // planes (4 fp16 per element) plus their row exponents and the BF16x3
+  // planes (6 bf16 per element, fewer than the 3xTF32 ones).
   const std::size_t tf32 = 4 * (m + n) * ((k + 7) / 8 * 8);
   const std::size_t fp16 = 2 * (m + n) * ((k + 15) / 16 * 16) + (m + n);
   return tf32 > fp16 ? tf32 : fp16;
@@ -852,9 +1032,9 @@ void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size
   const std::size_t kpad = (k + BK - 1) / BK * BK;
   float* pb = workspace + 4 * m * kpad * (std::size_t)batch;
   {
-    dim3 ga((unsigned)std::min<std::uint64_t>((m * k + 255) / 256, 152 * 16), (unsigned)batch);
+    dim3 ga((unsigned)std::min<std::uint64_t>((m + 7) / 8, 152 * 16), (unsigned)batch);
     split_tf32_kernel<<<ga, 256, 0, s>>>(A, pa, m, k, kpad, batch_stride);
-    dim3 gb((unsigned)std::min<std::uint64_t>((n * k + 255) / 256, 152 * 16), (unsigned)batch);
+    dim3 gb((unsigned)std::min<std::uint64_t>((n + 7) / 8, 152 * 16), (unsigned)batch);
     split_tf32_kernel<<<gb, 256, 0, s>>>(Bt, pb, n, k, kpad, bt_stride);
     check(cudaGetLastError(), "split_tf32");
   }
@@ -907,6 +1087,41 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
   cgemm_fp16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err,
                                                         cfg.chunk, ea, eb);
   check(cudaGetLastError(), "cgemm_fp16x3");
+}
+
+void launch_cgemm_bf16x3(const float2* A, const float2* Bt, float2* C, std::size_t m, std::size_t n,
+                         std::size_t k, std::uint64_t batch_stride, std::uint64_t bt_stride, int batch,
+                         float* workspace, int* err, const TcConfig& cfg, cudaStream_t s) {
+  if (!tc_eligible(m, n, k)) throw std::string("ERROR (qflex_gb300: tensor cores) --> shape not eligible");
+  if (cfg.chunk < 1 || cfg.chunk > 64)
+    throw std::string("ERROR (qflex_gb300: tensor cores) --> chunk length must be 1..64");
+  static std::once_flag attr;
+  std::call_once(attr, [] {
+    check(cudaFuncSetAttribute(cgemm_bf16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
+          "cudaFuncSetAttribute");
+  });
+  const std::size_t kpad = (k + 15) / 16 * 16;
+  const std::size_t nb = (std::size_t)batch;
+  __nv_bfloat16* am = reinterpret_cast<__nv_bfloat16*>(workspace);
+  __nv_bfloat16* at = am + 4 * m * kpad * nb;
+  __nv_bfloat16* bm = at + 2 * m * kpad * nb;
+  __nv_bfloat16* bt = bm + 4 * n * kpad * nb;
+  {
+    dim3 ga((unsigned)std::min<std::uint64_t>((m + 7) / 8, 152 * 16), (unsigned)batch);
+    split_bf16_kernel<<<ga, 256, 0, s>>>(A, am, at, m, k, kpad, batch_stride);
+    dim3 gb((unsigned)std::min<std::uint64_t>((n + 7) / 8, 152 * 16), (unsigned)batch);
+    split_bf16_kernel<<<gb, 256, 0, s>>>(Bt, bm, bt, n, k, kpad, bt_stride);
+    check(cudaGetLastError(), "split_bf16");
+  }
+  const CUtensorMap ma = plane_map_bf16(am, m, kpad, batch, BM, 64);
+  const CUtensorMap mb = plane_map_bf16(bm, n, kpad, batch, BN, 64);
+  const CUtensorMap ma2 = plane_map_bf16(at, m, kpad, batch, BM, 32);
+  const CUtensorMap mb2 = plane_map_bf16(bt, n, kpad, batch, BN, 32);
+  const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
+  dim3 grid((unsigned)tiles, 1, (unsigned)batch);
+  cgemm_bf16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, ma2, mb2, C, (int)m, (int)n, (int)k, batch_stride,
+                                                        err, cfg.chunk);
+  check(cudaGetLastError(), "cgemm_bf16x3");
 }
 
 }  // namespace qfx

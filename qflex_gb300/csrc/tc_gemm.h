@@ -40,4 +40,12 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
                          std::size_t k, std::uint64_t ac_stride, std::uint64_t bt_stride, int batch,
                          float* workspace, int* err, const TcConfig& cfg, cudaStream_t s);
 
+// The same product with BF16x3 planes: x = b0 + b1 + b2 in BF16 (no
+// scaling: BF16 has the FP32 exponent range), six products per real
+// product (x0y0, x0y1, x1y0, x0y2, x1y1, x2y0) on kind::f16 tensor cores.
+// Single-CTA kernel; cfg.variant is ignored.
+void launch_cgemm_bf16x3(const float2* A, const float2* Bt, float2* C, std::size_t m, std::size_t n,
+                         std::size_t k, std::uint64_t ac_stride, std::uint64_t bt_stride, int batch,
+                         float* workspace, int* err, const TcConfig& cfg, cudaStream_t s);
+
 }  // namespace qfx

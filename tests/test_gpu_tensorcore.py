@@ -1,5 +1,5 @@
-"""Split-precision tcgen05 products (3xTF32, and 3xFP16 with power-of-two
-row scaling) and the engine in those modes; every test runs for both.
+"""Split-precision tcgen05 products (3xTF32, 3xFP16 with power-of-two row
+scaling, BF16x3) and the engine in those modes; every test runs for each.
 Tolerance: per-amplitude error within 1e-5 of the RMS amplitude against
 the reference's complex<float> results and the FP64 oracle; products within
 2e-5 of the FP64 product relative to its mean magnitude (the FP32
@@ -8,14 +8,14 @@ import numpy as np
 import pytest
 
 from oracle import qflex_oracle as qo
-from qflex_gb300 import FP16X3, TF32X3, Context, rqc
+from qflex_gb300 import BF16X3, FP16X3, TF32X3, Context, rqc
 from tests.conftest import rel_err
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-5
 
 
-@pytest.fixture(scope="module", params=[TF32X3, FP16X3], ids=["tf32x3", "fp16x3"])
+@pytest.fixture(scope="module", params=[TF32X3, FP16X3, BF16X3], ids=["tf32x3", "fp16x3", "bf16x3"])
 def tc_ctx(built_lib, request):
     return Context(0, request.param)
 
