@@ -39,7 +39,7 @@ WORKLOAD = "c3"
 FP32_PEAK_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12  # TFLOP/s, FP32 CUDA-core FMA
 # DRAM bytes (read + write) of one launch of the dominant product, from ncu
 # captures summarised in profiles/.
-TRAFFIC = {("tf32x3", 4096, 4096, 4096): 2.322e9}
+TRAFFIC = {("tf32x3", 4096, 4096, 4096): 2.322e9, ("fp16x3", 4096, 4096, 4096): 0.991e9}
 
 
 def parse():
