@@ -129,6 +129,11 @@ size_t qflex_gb300_last_ops(const qflex_gb300_context* ctx, double* out, size_t 
  *                replay it (default 1, or QFLEX_GB300_GRAPHS)
  *   "max_batch"  most output strings per device pass of evaluate_many
  *                (0: as many as fit in device memory; default 0)
+ *   "open_terminals" 1: terminal cuts that take all their values, with no
+ *                two-qubit cut after them, stay open indices -- the ops after
+ *                them run once on tensors carrying the open indices instead
+ *                of once per terminal value (same amplitudes); 0: the
+ *                reference's projection per value (default 1)
  * Unknown names and out-of-range values return QFLEX_GB300_ERR_ARG. */
 int qflex_gb300_set_option(qflex_gb300_context* ctx, const char* name, double value);
 int qflex_gb300_get_option(const qflex_gb300_context* ctx, const char* name, double* value);

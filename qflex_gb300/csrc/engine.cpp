@@ -118,6 +118,9 @@ void Engine::set_option(const std::string& name, double value) {
   } else if (name == "graphs") {
     if (value != 0 && value != 1) throw QFX_ERR("Option graphs must be 0 or 1.");
     graphs_ = value != 0;
+  } else if (name == "open_terminals") {
+    if (value != 0 && value != 1) throw QFX_ERR("Option open_terminals must be 0 or 1.");
+    open_terminals_ = value != 0;
   } else if (name == "max_batch") {
     if (!(value >= 0 && value <= 65535) || value != double(int(value)))
       throw QFX_ERR("Option max_batch must be an integer in 0..65535.");
@@ -133,6 +136,7 @@ double Engine::get_option(const std::string& name) const {
   if (name == "tc_pair") return tc_cfg_.variant == 0 ? 0 : 1;
   if (name == "graphs") return graphs_ ? 1 : 0;
   if (name == "max_batch") return max_batch_;
+  if (name == "open_terminals") return open_terminals_ ? 1 : 0;
   throw QFX_ERR("Unknown option '", name, "'.");
 }
 
@@ -249,6 +253,7 @@ Engine::Plan* Engine::get_plan(const std::string& circuit, const std::string& or
   key += grid;
   key += '\x01';
   key += std::to_string(precision_);
+  key += open_terminals_ ? "o" : "p";
   if (plan_ && plan_->key == key) return plan_.get();
   auto p = std::make_unique<Plan>();
   p->key = std::move(key);
@@ -427,7 +432,7 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
     std::function<bool(std::size_t, std::size_t, std::size_t)> b_kmajor;
     if (precision_ != FP32) b_kmajor = tc_eligible;
     try {
-      p.prog = plan_contraction(p.net, p.ops, results[0].states.size(), INFINITY, b_kmajor);
+      p.prog = plan_contraction(p.net, p.ops, results[0].states.size(), INFINITY, b_kmajor, open_terminals_);
     } catch (const std::string& e) {
       throw QFX_WRAP("ContractGrid", e);
     }

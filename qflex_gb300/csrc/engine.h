@@ -114,6 +114,7 @@ class Engine {
   TcConfig tc_cfg_;
   std::map<std::tuple<std::size_t, std::size_t, std::size_t>, int> tc_variant_;
   int max_batch_ = 0;            // output strings per device pass (0: as many as fit)
+  bool open_terminals_ = true;   // terminal cuts as open indices where the planner can
   unsigned options_version_ = 0;  // part of the graph key: options change launches
   TcConfig tc_config(std::size_t m, std::size_t n, std::size_t k) const;
   // C = A * Bt^T on the tensor cores in the context's split precision.

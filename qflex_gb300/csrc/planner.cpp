@@ -135,9 +135,32 @@ double reference_plan_bytes(const Network& net, const std::vector<Op>& ops) {
 class Planner {
  public:
   Planner(const Network& net, const std::vector<Op>& ops, std::size_t n_amps,
-          std::function<bool(std::size_t, std::size_t, std::size_t)> b_kmajor)
+          std::function<bool(std::size_t, std::size_t, std::size_t)> b_kmajor, bool open_terminals)
       : net_(net), ops_(ops), b_kmajor_(std::move(b_kmajor)) {
     prog_.n_amplitudes = n_amps;
+    // Terminal cuts stay open indices when every one of them takes all its
+    // values and no two-qubit cut follows the first of them: the ops after
+    // them then run once on tensors that carry the open (o) indices, and
+    // the final tensor holds all the region's amplitudes, instead of the
+    // reference's re-run of those ops per terminal value
+    // (src/contraction_utils.cpp:300-314).
+    open_ = open_terminals;
+    bool seen_terminal = false;
+    for (const auto& op : ops_) {
+      if (op.kind != Op::CUT) continue;
+      if (op.tensors.size() == 1) {
+        seen_terminal = true;
+        if (!op.values.empty()) {
+          bool full = op.values.size() == 2;
+          for (std::size_t v = 0; v < op.values.size() && full; ++v) full = op.values[v] == v;
+          if (!full) open_ = false;
+        }
+        open_order_.push_back(cut_index_name(op));
+      } else if (seen_terminal) {
+        open_ = false;
+      }
+    }
+    if (open_order_.empty()) open_ = false;
   }
 
   Program run() {
@@ -156,7 +179,7 @@ class Planner {
     prog_.n_leaves = leaves_;
     prog_.arena_elems = top_ + round_up(std::max<std::size_t>(leaves_, 1));
     for (auto& op : prog_.ops)
-      if (op.kind == DevOp::GEMM && op.c >= kLeafMark) op.c = prog_.results_offset + (op.c - kLeafMark);
+      if (op.c >= kLeafMark) op.c = prog_.results_offset + (op.c - kLeafMark);
     for (auto& [key, idx] : shape_index_) prog_.shapes[idx].count = shape_count_[idx];
     return std::move(prog_);
   }
@@ -205,7 +228,7 @@ class Planner {
 
   // Moves the data of `t` into index order `order` (an out-of-place
   // permute into a fresh buffer) unless it is already laid out that way.
-  void physical(STensor& t, const std::vector<std::string>& order) {
+  void physical(STensor& t, const std::vector<std::string>& order, std::size_t leaf_dst = 0) {
     if (order.empty() && t.phys.empty()) return;
     if (order == t.phys) return;
     const std::size_t r = t.phys.size();
@@ -231,9 +254,9 @@ class Planner {
     bool identity = true;
     for (int b = 0; b < nbits; ++b) identity &= (op.perm[b] == b);
     if (!identity) {
-      const int nb = alloc(t.size());
+      const int nb = leaf_dst ? -1 : alloc(t.size());
       op.a = addr(t);
-      op.c = bufs_[nb].off;
+      op.c = leaf_dst ? leaf_dst : bufs_[nb].off;
       prog_.permute_bytes += 16.0 * double(t.size());
       prog_.ops.push_back(op);
       decref(t.buf);
@@ -301,6 +324,17 @@ class Planner {
     bool have_output = false;
     STensor output;
     std::size_t output_op = 0;
+    // Grid tensors of open terminal cuts, restored when this slice is done
+    // (the products after the cut reorder them in place, as the reference
+    // reorders its projected copies).
+    std::vector<std::pair<Coord, STensor>> saved;
+    auto restore = [&]() {
+      for (auto& [pos_, t] : saved) {
+        assign(grid_.at(pos_), t);
+        decref(t.buf);
+      }
+      saved.clear();
+    };
     while (pos < ops_.size()) {
       const Op& op = ops_[pos++];
       const bool last = pos == ops_.size();
@@ -323,6 +357,20 @@ class Planner {
       } else if (op.kind == Op::CUT) {
         const std::string index = cut_index_name(op);
         STensor& ta = grid_.at(op.tensors[0]);
+        if (open_ && op.tensors.size() == 1) {
+          // Open terminal index: the checks of the projection, no
+          // projection; the index stays on the tensor for the ops after it.
+          if (std::find(ta.idx.begin(), ta.idx.end(), index) == ta.idx.end())
+            throw QFX_ERR("Index ", index, " is not an index of the tensor at (", op.tensors[0].first, ",",
+                          op.tensors[0].second, ").");
+          if (index != ta.idx[0])
+            throw QFX_ERR("Failed to call project(). Error:\n\t[Index: '", index,
+                          "' has to be equal to indices[0]: '", ta.idx[0], "'.]");
+          out_idx *= op.values.empty() ? ta.dim_of(index) : op.values.size();
+          saved.emplace_back(op.tensors[0], STensor{});
+          assign(saved.back().second, ta);
+          continue;
+        }
         STensor copy_a;
         assign(copy_a, ta);
         lead_with(copy_a, index);
@@ -375,6 +423,29 @@ class Planner {
     }
     if (!have_output)
       throw QFX_ERR("Contraction did not complete; the ordering does not end with a product.");
+    if (open_) {
+      // The final tensor carries the open terminal indices: lay it out in
+      // cut order (first cut most significant, as the output states are
+      // numbered) straight into the results region.
+      std::vector<std::string> sorted_idx = output.idx, sorted_open = open_order_;
+      std::sort(sorted_idx.begin(), sorted_idx.end());
+      std::sort(sorted_open.begin(), sorted_open.end());
+      if (sorted_idx != sorted_open)
+        throw QFX_ERR("Contraction did not complete; final tensor is: ", output.describe());
+      const std::size_t count = output.size();
+      if (out_idx + count > prog_.n_amplitudes)
+        throw QFX_ERR("Output index ", out_idx + count - 1, " exceeds the ", prog_.n_amplitudes,
+                      " output states.");
+      if (output.phys == open_order_)
+        prog_.ops[output_op].c = kLeafMark + leaves_;
+      else
+        physical(output, open_order_, kLeafMark + leaves_);
+      for (std::size_t v = 0; v < count; ++v) prog_.leaf_amp.push_back((std::uint32_t)(out_idx + v));
+      leaves_ += count;
+      decref(output.buf);
+      restore();
+      return;
+    }
     if (output.size() != 1)
       throw QFX_ERR("Contraction did not complete; final tensor is: ", output.describe());
     if (out_idx >= prog_.n_amplitudes)
@@ -431,6 +502,8 @@ class Planner {
   std::vector<int> free_[64];
   std::size_t top_ = 0;
   std::size_t leaves_ = 0;
+  bool open_ = false;                    // terminal cuts kept as open indices
+  std::vector<std::string> open_order_;  // their index names in cut order
   std::map<Coord, STensor> grid_;
   std::unordered_map<std::string, STensor> scratch_;
   std::map<std::tuple<std::size_t, std::size_t, std::size_t>, int> shape_index_;
@@ -441,14 +514,15 @@ class Planner {
 
 Program plan_contraction(const Network& net, const std::vector<Op>& ops, std::size_t n_amplitudes,
                          double memory_limit,
-                         std::function<bool(std::size_t, std::size_t, std::size_t)> b_kmajor) {
+                         std::function<bool(std::size_t, std::size_t, std::size_t)> b_kmajor,
+                         bool open_terminals) {
   const double ref_bytes = reference_plan_bytes(net, ops);
   if (ref_bytes > memory_limit)
     throw QFX_ERR("Failed to call Initialize(). Error:\n\t[Required space (",
                   readable_memory_string(ref_bytes), ") exceeds memory limit (",
                   readable_memory_string(memory_limit), "). Cancelling simulation.]");
   if (!b_kmajor) b_kmajor = [](std::size_t, std::size_t, std::size_t) { return false; };
-  Planner p(net, ops, n_amplitudes, std::move(b_kmajor));
+  Planner p(net, ops, n_amplitudes, std::move(b_kmajor), open_terminals);
   Program prog = p.run();
   prog.reference_bytes = ref_bytes;
   return prog;

@@ -58,8 +58,12 @@ struct Program {
 // `b_kmajor(m, n, k)` tells whether the product of that shape runs on a
 // kernel that reads B as [n][k] rows (the tensor-core path); by default
 // every product reads the reference's [k][n] layout.
+// With `open_terminals`, terminal cuts that take all their values (and are
+// not followed by a two-qubit cut) stay open indices: the ops after them
+// run once and the final tensor holds the terminal region's amplitudes.
 Program plan_contraction(const Network& net, const std::vector<Op>& ops,
                          std::size_t n_amplitudes, double memory_limit,
-                         std::function<bool(std::size_t, std::size_t, std::size_t)> b_kmajor = {});
+                         std::function<bool(std::size_t, std::size_t, std::size_t)> b_kmajor = {},
+                         bool open_terminals = false);
 
 }  // namespace qfx

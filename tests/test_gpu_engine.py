@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from oracle import qflex_oracle as qo
-from qflex_gb300 import QflexGb300Error, rqc, simulate
+from qflex_gb300 import Context, QflexGb300Error, rqc, simulate
 from tests.conftest import rel_err
 
 pytestmark = pytest.mark.gpu
@@ -203,3 +203,26 @@ def test_simulate_drop_in(built_lib, ref_cases, capsys):
                     "memory_limit": 512})  # the plan needs 832 bytes
     assert bad == []
     assert "exceeds memory limit" in capsys.readouterr().err
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16x3"])
+def test_open_terminals_match_projection_and_fp64(built_lib, precision):
+    """Terminal cuts as open indices give the amplitudes of the reference's
+    projection per value (both engine modes) and of the FP64 oracle."""
+    from tests.test_host_planner import _terminal_case
+    c, o, g, ini, finals = _terminal_case(3)
+    opened, projected = Context(0), Context(0)
+    opened.set_precision(precision)
+    projected.set_precision(precision)
+    projected.set_option("open_terminals", 0)
+    a = opened.evaluate_many(c, o, g, ini, finals, 1 << 40)
+    b = projected.evaluate_many(c, o, g, ini, finals, 1 << 40)
+    assert [s for s, _ in a] == [s for s, _ in b] and len(a) == 8 * len(finals)
+    assert opened.stats()["n_ops"] < projected.stats()["n_ops"]
+    want = []
+    for f in finals:
+        inp = qo.Input(qo.Circuit.loads(c), qo.load_ordering(o), qo.Grid.loads(g), ini, f)
+        want += qo.evaluate_circuit(inp, np.complex128, float(1 << 40))
+    assert [s for s, _ in a] == [s for s, _ in want]
+    assert rel_err([x for _, x in a], [x for _, x in b]) < FP32_TOL
+    assert rel_err([x for _, x in a], [x for _, x in want]) < FP32_TOL

@@ -6,12 +6,17 @@ import numpy as np
 import pytest
 
 from oracle import qflex_oracle as qo
-from qflex_gb300 import Context, QflexGb300Error, rqc
+from qflex_gb300 import FP32, Context, QflexGb300Error, rqc
 
 
 @pytest.fixture(scope="module")
 def plan_ctx(built_lib):
-    return Context(-1)
+    """Planning-only context that contracts exactly as the reference does
+    (terminal cuts projected per value), so its products are the
+    reference's CBLAS calls."""
+    ctx = Context(-1)
+    ctx.set_option("open_terminals", 0)
+    return ctx
 
 
 CASES = ["simple", "c1_4x5_d16", "rect4x4_cut_terminal", "c2_6x6_d24_partial_cut",
@@ -110,3 +115,50 @@ def test_workload_plans(plan_ctx):
         s = plan_ctx.stats()
         assert s["arena_bytes"] < max_gb * 2 ** 30
         assert s["gemm_flop"] > 0
+
+
+def _terminal_case(n_terminal=3):
+    """4x5 (1+16+1) circuit: a row sweep of the first qubits into patch a,
+    terminal cuts on the last `n_terminal` qubits, which patch b takes
+    before it merges into a."""
+    c, _, g, ini, fins = rqc.workload("c1", seed=9)
+    qs = list(range(20))
+    term = qs[-n_terminal:]
+    lines = [f"expand a {q}" for q in qs[:-n_terminal]]
+    lines += [f"cut () {q}" for q in term]
+    lines += [f"expand b {q}" for q in term] + ["merge a b"]
+    finals = []
+    for f in fins[:3]:
+        f = list(f)
+        for q in term:
+            f[q] = "x"
+        finals.append("".join(f))
+    return c, "\n".join(lines) + "\n", g, ini, finals
+
+
+def test_open_terminal_plan_matches_projection(built_lib):
+    """Terminal cuts as open indices: same output states, far fewer ops,
+    the same amplitude for every leaf's value."""
+    c, o, g, ini, finals = _terminal_case(3)
+    res = {}
+    for mode in (0, 1):
+        plan = Context(-1, FP32)
+        plan.set_option("open_terminals", mode)
+        out = plan.evaluate(c, o, g, ini, finals[0], 1 << 40)
+        res[mode] = ([s for s, _ in out], plan.stats())
+    assert res[0][0] == res[1][0] and len(res[0][0]) == 8
+    assert res[1][1]["n_leaves"] == res[0][1]["n_leaves"] == 8
+    assert res[1][1]["n_ops"] < res[0][1]["n_ops"]
+
+
+def test_open_terminals_fall_back_to_projection(built_lib):
+    """A partial value list on a terminal cut keeps the reference's
+    projection per value (same plan with the option on or off)."""
+    c, o, g, ini, finals = _terminal_case(2)
+    partial = o.replace("cut () 19", "cut (1) 19")
+    p0, p1 = Context(-1, FP32), Context(-1, FP32)
+    p0.set_option("open_terminals", 0)
+    a = p0.evaluate(c, partial, g, ini, finals[0], 1 << 40)
+    b = p1.evaluate(c, partial, g, ini, finals[0], 1 << 40)
+    assert [s for s, _ in a] == [s for s, _ in b] and len(a) == 2
+    assert p0.stats()["n_ops"] == p1.stats()["n_ops"]
