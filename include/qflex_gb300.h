@@ -122,9 +122,9 @@ size_t qflex_gb300_last_ops(const qflex_gb300_context* ctx, double* out, size_t 
  *                tensor-core product, 1..64 (default 2, or QFLEX_TC_CHUNK;
  *                longer chunks are faster and less accurate: the tensor
  *                core's FP32 accumulation truncates)
- *   "tc_pair"    1: products with m >= 256 use the CTA-pair (cta_group::2,
- *                256 x 128 tile) kernel; 0: every product uses the
- *                single-CTA 128 x 128 tile (default 1, or QFLEX_TC_PAIR)
+ *   "tc_pair"    1: 3xTF32 products with m >= 256 use the CTA-pair
+ *                (cta_group::2, 256 x 128 tile) kernel; 0: every product uses
+ *                the single-CTA 128 x 128 tile (default 0, or QFLEX_TC_PAIR)
  *   "graphs"     1: capture a repeated device pass in a CUDA graph and
  *                replay it (default 1, or QFLEX_GB300_GRAPHS)
  *   "max_batch"  most output strings per device pass of evaluate_many

@@ -363,7 +363,7 @@ std::size_t Engine::run_program(Plan& p, int batch, float2* arena, float* tc_ws)
     } else {
       launch_cgemm_fp32(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, batch,
                         stream_, scratch);
-      launches += skinny_splits(op.m, op.n, op.k, batch) ? 2 : 1;
+      launches += (vm_splits(op.m, op.n, op.k, batch) || skinny_splits(op.m, op.n, op.k, batch)) ? 2 : 1;
     }
   }
   if (profile_) QFX_CUDA(cudaEventRecord(prof_events_[prog.ops.size()], stream_));
@@ -383,7 +383,8 @@ std::vector<OpRecord> Engine::last_ops() const {
       r.n = r.k = 1;
       r.bytes = 16.0 * r.m;
     } else {
-      r.kind = op.b_nk ? 2 : (skinny_splits(op.m, op.n, op.k, (int)std::max<std::size_t>(stats_.batch, 1)) ? 3 : 1);
+      const int nb = (int)std::max<std::size_t>(stats_.batch, 1);
+      r.kind = op.b_nk ? 2 : ((vm_splits(op.m, op.n, op.k, nb) || skinny_splits(op.m, op.n, op.k, nb)) ? 3 : 1);
       r.m = double(op.m);
       r.n = double(op.n);
       r.k = double(op.k);

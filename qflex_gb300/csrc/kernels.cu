@@ -381,6 +381,43 @@ __global__ void __launch_bounds__(256) skinny_partial(const float2* __restrict__
   }
 }
 
+// C[1][n] = A[1][k] * B[k][n] for 2 <= n <= 256 and long k (the vector
+// times matrix products of multiply, src/tensor.cpp:1144-1150): block s sums
+// rows [k0, k1) of B for all n columns at once. R = 256 / n rows per pass,
+// thread t on column t % n of row t / n, so every pass reads R whole rows
+// of B (coalesced) and A once; the R row partials of each column are added
+// in row order into partial[(b * n + j) * splits + s], which skinny_finish
+// adds up in FP64.
+__global__ void __launch_bounds__(256) vm_partial(const float2* __restrict__ A, const float2* __restrict__ B,
+                                                  float2* __restrict__ partial, int n, std::uint64_t k, int splits,
+                                                  std::uint64_t batch_stride) {
+  __shared__ float2 red[256];
+  const int s = blockIdx.x;
+  const std::uint64_t boff = std::uint64_t(blockIdx.y) * batch_stride;
+  const std::uint64_t chunk = (k + splits - 1) / splits;
+  const std::uint64_t k0 = std::uint64_t(s) * chunk;
+  const std::uint64_t k1 = k0 + chunk < k ? k0 + chunk : k;
+  const int R = 256 / n;
+  const int t = threadIdx.x, r = t / n, j = t % n;
+  float2 acc = make_float2(0.f, 0.f);
+  if (r < R) {
+    const float2* a = A + boff;
+    const float2* b = B + boff + j;
+#pragma unroll 4
+    for (std::uint64_t kk = k0 + r; kk < k1; kk += R) acc = cfma(a[kk], b[kk * n], acc);
+  }
+  red[t] = acc;
+  __syncthreads();
+  if (t < n) {
+    float2 v = red[t];
+    for (int q = 1; q < R; ++q) {
+      v.x += red[q * n + t].x;
+      v.y += red[q * n + t].y;
+    }
+    partial[(std::uint64_t(blockIdx.y) * n + t) * splits + s] = v;
+  }
+}
+
 // One warp per output: lane l adds partials l, l + 32, ... in FP64, then a
 // fixed shuffle tree combines the lanes.
 __global__ void skinny_finish(const float2* __restrict__ partial, float2* __restrict__ C, int outputs,
@@ -554,6 +591,13 @@ void launch_permute(const PermPlan& plan, const float2* src, float2* dst, std::u
   check_launch("permute");
 }
 
+int vm_splits(std::size_t m, std::size_t n, std::size_t k, int batch) {
+  if (m != 1 || n < 2 || n > 256 || k < 4096) return 0;
+  std::size_t splits = std::min<std::size_t>(4096, k / 2048);
+  while (splits > 1 && splits * n * (std::size_t)batch > kSkinnyScratchElems) splits /= 2;
+  return splits >= 2 ? (int)splits : 0;
+}
+
 int skinny_splits(std::size_t m, std::size_t n, std::size_t k, int batch) {
   if (m * n > 64 || k < 8192) return 0;
   std::size_t splits = std::min<std::size_t>(2048, (k + 4095) / 4096);
@@ -575,6 +619,15 @@ void launch_skinny_split(const float2* A, const float2* B, float2* C, std::size_
 void launch_cgemm_fp32(const float2* A, const float2* B, float2* C, std::size_t m, std::size_t n,
                        std::size_t k, std::uint64_t stride, int batch, cudaStream_t s,
                        float2* scratch) {
+  if (const int splits = scratch ? vm_splits(m, n, k, batch) : 0) {
+    dim3 g1((unsigned)splits, (unsigned)batch);
+    vm_partial<<<g1, 256, 0, s>>>(A, B, scratch, (int)n, k, splits, stride);
+    check_launch("vm_partial");
+    dim3 g2((unsigned)((n * 32 + 127) / 128), (unsigned)batch);
+    skinny_finish<<<g2, 128, 0, s>>>(scratch, C, (int)n, splits, stride);
+    check_launch("skinny_finish");
+    return;
+  }
   if (const int splits = scratch ? skinny_splits(m, n, k, batch) : 0) {
     const int outputs = (int)(m * n);
     dim3 g1((unsigned)(outputs * splits), (unsigned)batch);

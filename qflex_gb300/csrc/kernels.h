@@ -86,6 +86,10 @@ void launch_permute(const PermPlan& plan, const float2* src, float2* dst, std::u
 // float2, or nullptr to keep the one-block-per-output kernels).
 constexpr std::size_t kSkinnyScratchElems = std::size_t(1) << 20;
 int skinny_splits(std::size_t m, std::size_t n, std::size_t k, int batch);
+// Vector-times-matrix products (m = 1, 2 <= n <= 256, long k) split k over
+// blocks that each read whole rows of B; 0 when the shape does not qualify.
+// Takes precedence over skinny_splits.
+int vm_splits(std::size_t m, std::size_t n, std::size_t k, int batch);
 void launch_cgemm_fp32(const float2* A, const float2* B, float2* C, std::size_t m, std::size_t n,
                        std::size_t k, std::uint64_t batch_stride, int batch, cudaStream_t s,
                        float2* scratch);

@@ -1007,8 +1007,10 @@ TcConfig tc_default_config() {
     const int v = std::atoi(e);
     if (v >= 1 && v <= 64) c.chunk = v;
   }
+  // The single-CTA tile measured faster on every product of the 7x7
+  // (1+32+1) plan; QFLEX_TC_PAIR=1 sends products with m >= 256 to the pair.
   if (const char* e = std::getenv("QFLEX_TC_PAIR"))
-    if (std::atoi(e) == 0) c.variant = 0;
+    if (std::atoi(e) == 1) c.variant = -1;
   return c;
 }
 

@@ -73,7 +73,9 @@ def test_reorder_in_place(gpu_ctx):
 
 SHAPES = [(1, 1, 1), (2, 4, 2), (16, 1, 2), (1, 4, 4), (3, 5, 7), (64, 64, 64), (130, 70, 33),
           (256, 16, 16), (16, 256, 16), (4096, 1, 64), (1, 4096, 64), (1, 1, 100000),
-          (2, 3, 50000), (513, 257, 129), (1024, 16, 16), (8, 300, 9)]
+          (2, 3, 50000), (513, 257, 129), (1024, 16, 16), (8, 300, 9),
+          # vector times matrix with long k: the split-k row-reading kernel
+          (1, 64, 1 << 16), (1, 2, 8192), (1, 200, 5000), (1, 256, 4096)]
 
 
 @pytest.mark.parametrize("m,n,k", SHAPES)

@@ -20,8 +20,7 @@ def tc_ctx(built_lib, request):
     return Context(0, request.param)
 
 
-# m < 256 runs on the single-CTA kernel, m >= 256 on the CTA-pair kernel;
-# ragged m and n leave whole CTAs of a pair outside the matrix.
+# Ragged m and n leave whole tiles partly outside the matrix.
 @pytest.mark.parametrize("m,n,k", [(128, 128, 16), (64, 64, 16), (256, 512, 128), (1024, 256, 256),
                                    (300, 128, 64), (128, 1024, 40), (4096, 256, 256), (256, 64, 16),
                                    (512, 96, 24), (768, 200, 100), (2048, 2048, 2048)])
@@ -133,3 +132,23 @@ def test_fp16x3_rows_of_any_magnitude(built_lib):
     ok = np.isfinite(scale) & (scale > 1e-36) & (scale < 1e36)  # products FP32 can hold
     err = np.abs(got - want) / scale
     assert np.max(err[ok]) < 2e-5, np.max(err[ok])
+
+
+@pytest.mark.parametrize("m,n,k", [(256, 128, 16), (300, 128, 64), (512, 96, 24), (1024, 256, 256)])
+def test_tf32x3_pair_kernel(built_lib, m, n, k):
+    """The CTA-pair (cta_group::2) 3xTF32 kernel, ragged shapes included."""
+    import torch
+    ctx = Context(0, TF32X3)
+    ctx.set_option("tc_pair", 1)
+    g = np.random.default_rng(m + n + k)
+    A = (g.standard_normal((m, k)) + 1j * g.standard_normal((m, k))).astype(np.complex64)
+    B = (g.standard_normal((k, n)) + 1j * g.standard_normal((k, n))).astype(np.complex64)
+    dA, dB = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+    dC = torch.full((m, n), float("nan"), dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()
+    ctx.multiply(dA.data_ptr(), dB.data_ptr(), dC.data_ptr(), m, n, k)
+    ctx.synchronize()
+    got = dC.cpu().numpy()
+    want = A.astype(np.complex128) @ B.astype(np.complex128)
+    assert np.isfinite(got).all()
+    assert np.max(np.abs(got - want)) / np.mean(np.abs(want)) < 2e-5
