@@ -47,7 +47,7 @@ namespace qfx {
 namespace {
 
 constexpr int BM = 128, BN = 128, BK = 8;
-constexpr int STAGES = 6;
+constexpr int STAGES = 5;
 // One k-step of an operand tile: every row holds the four planes' 8 values
 // side by side (4 x 32 bytes = one 128-byte row in the 128-byte swizzle),
 // so plane p is the K-major matrix starting 32 p bytes into the tile.
@@ -57,8 +57,8 @@ constexpr int STAGE_BYTES = TILE_A + TILE_B;
 constexpr int EPI_WARPS = 8;
 constexpr int TMEM_COLS = 4 * BN;         // two chunk buffers of (re, im)
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-static_assert(BM * (BN + 1) * 8 <= STAGES * STAGE_BYTES, "the output tile is staged in the operand stages");
+constexpr int STAGING_BYTES = 8 * 32 * 32 * 8;  // 32 x 32 complex64 per epilogue warp
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + STAGING_BYTES + 1024 + 256;
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s per wait
 
 __device__ __forceinline__ std::uint32_t smem_u32(const void* p) {
@@ -204,46 +204,55 @@ __device__ __forceinline__ void mbar_arrive(std::uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// The single-CTA kernel body. KIND_FP16 operands carry per-row scale
-// exponents (value = plane value * 2^-e); the epilogue removes them.
-// KIND_BF16 operands have six planes per k-step: b0, b1 of re and im in a
-// 128-byte row (map_a / map_b) and b2 of re and im in a 64-byte row
-// (map_a2 / map_b2); its stages are 48 KB, four of them.
+// The single-CTA kernel body, persistent: CTA b takes output tiles b,
+// b + gridDim.x, ... (grouped raster, batch entries after each other), and
+// its producer, MMA issuer and epilogue run through the tiles on shared
+// stage and chunk counters, so one tile's epilogue overlaps the next tile's
+// loads and MMAs. KIND_FP16 operands carry per-row scale exponents (value =
+// plane value * 2^-e); the epilogue removes them. KIND_BF16 operands have
+// six planes per k-step: b0, b1 of re and im in a 128-byte row (map_a /
+// map_b) and b2 of re and im in a 64-byte row (map_a2 / map_b2).
 template <int KIND>
 __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const CUtensorMap* map_b,
                                                  const CUtensorMap* map_a2, const CUtensorMap* map_b2,
-                                                 float2* __restrict__ C, int m, int n, int k,
+                                                 float2* __restrict__ C, int m, int n, int k, int batches,
                                                  std::uint64_t c_batch_stride, int* __restrict__ err, int CHUNK,
                                                  const int* __restrict__ exp_a,
                                                  const int* __restrict__ exp_b) {
   constexpr int KSTEP = KIND == KIND_TF32 ? 8 : 16;  // k values per plane row of 32 bytes
   constexpr int TAIL = BM * 64;                       // BF16 third-piece tile of one operand
-  constexpr int NST = KIND == KIND_BF16 ? 4 : STAGES;
+  constexpr int NST = KIND == KIND_BF16 ? 3 : STAGES;
   constexpr int SBYTES = KIND == KIND_BF16 ? 2 * (TILE_A + TAIL) : STAGE_BYTES;
   static_assert(NST * SBYTES <= STAGES * STAGE_BYTES, "stages fit the shared memory of the launch");
-  static_assert(BM * (BN + 1) * 8 <= NST * SBYTES, "the output tile is staged in the operand stages");
   extern __shared__ __align__(1024) std::uint8_t smem_raw[];
   std::uint8_t* smem = reinterpret_cast<std::uint8_t*>((reinterpret_cast<std::uintptr_t>(smem_raw) + 1023) &
                                                        ~std::uintptr_t(1023));
-  std::uint64_t* full = reinterpret_cast<std::uint64_t*>(smem + NST * SBYTES);
+  // Output staging, 32 x 32 complex64 per epilogue warp (XOR-swizzled).
+  float2* staging = reinterpret_cast<float2*>(smem + STAGES * STAGE_BYTES);
+  std::uint64_t* full = reinterpret_cast<std::uint64_t*>(smem + STAGES * STAGE_BYTES + STAGING_BYTES);
   std::uint64_t* empty = full + NST;
-  std::uint64_t* acc_full = empty + NST;   // [2]: a chunk accumulator is complete
-  std::uint64_t* acc_empty = acc_full + 2;    // [2]: a chunk accumulator was drained
-  std::uint64_t* mma_done = acc_empty + 2;    // every issued MMA has completed
+  std::uint64_t* acc_full = empty + NST;    // [2]: a chunk accumulator is complete
+  std::uint64_t* acc_empty = acc_full + 2;  // [2]: a chunk accumulator was drained
+  std::uint64_t* mma_done = acc_empty + 2;  // every issued MMA has completed
   std::uint32_t* tmem_slot = reinterpret_cast<std::uint32_t*>(mma_done + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  // Tiles run in groups of 8 row-tiles so that the CTAs resident at one
-  // time share A rows and B columns in L2.
   const int tiles_m = (m + BM - 1) / BM;
   const int tiles_n = (n + BN - 1) / BN;
-  const int per_group = 8 * tiles_n;
-  const int group = blockIdx.x / per_group, in_group = blockIdx.x % per_group;
-  const int group_m = min(8, tiles_m - group * 8);
-  const int m0 = (group * 8 + in_group % group_m) * BM;
-  const int n0 = (in_group / group_m) * BN;
-  const int batch = blockIdx.z;
+  const int per_batch = tiles_m * tiles_n;
+  const int total = per_batch * batches;
+  // Tiles run in groups of 8 row-tiles so that the CTAs working at one time
+  // share A rows and B columns in L2.
+  auto tile_of = [&](int t, int& m0, int& n0, int& batch) {
+    batch = t / per_batch;
+    const int r = t % per_batch;
+    const int per_group = 8 * tiles_n;
+    const int group = r / per_group, in_group = r % per_group;
+    const int group_m = min(8, tiles_m - group * 8);
+    m0 = (group * 8 + in_group % group_m) * BM;
+    n0 = (in_group / group_m) * BN;
+  };
   const int kblocks = (k + KSTEP - 1) / KSTEP;
   const int chunks = (kblocks + CHUNK - 1) / CHUNK;
 
@@ -271,110 +280,126 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
   const std::uint32_t tmem = *tmem_slot;
 
   if (warp == 0 && lane == 0) {
-    // Producer.
-    int issued = 0;
-    for (int kb = 0; kb < kblocks; ++kb) {
-      const int s = kb % NST;
-      if (kb >= NST && !mbar_wait(&empty[s], ((kb / NST) - 1) & 1, abort_flag, err, 1)) break;
-      std::uint8_t* st = smem + s * SBYTES;
-      mbar_expect_tx(&full[s], SBYTES);
-      tma_load_4d(map_a, &full[s], st, 0, m0, kb, batch);
-      tma_load_4d(map_b, &full[s], st + TILE_A, 0, n0, kb, batch);
-      if constexpr (KIND == KIND_BF16) {
-        tma_load_4d(map_a2, &full[s], st + 2 * TILE_A, 0, m0, kb, batch);
-        tma_load_4d(map_b2, &full[s], st + 2 * TILE_A + TAIL, 0, n0, kb, batch);
+    // Producer: stage g % NST of the CTA-wide k-step count g.
+    int g = 0;
+    for (int t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x) {
+      int m0, n0, batch;
+      tile_of(t, m0, n0, batch);
+      for (int kb = 0; kb < kblocks; ++kb, ++g) {
+        const int s = g % NST;
+        if (g >= NST && !mbar_wait(&empty[s], ((g / NST) - 1) & 1, abort_flag, err, 1)) break;
+        std::uint8_t* st = smem + s * SBYTES;
+        mbar_expect_tx(&full[s], SBYTES);
+        tma_load_4d(map_a, &full[s], st, 0, m0, kb, batch);
+        tma_load_4d(map_b, &full[s], st + TILE_A, 0, n0, kb, batch);
+        if constexpr (KIND == KIND_BF16) {
+          tma_load_4d(map_a2, &full[s], st + 2 * TILE_A, 0, m0, kb, batch);
+          tma_load_4d(map_b2, &full[s], st + 2 * TILE_A + TAIL, 0, n0, kb, batch);
+        }
       }
-      issued = kb + 1;
     }
     if (*abort_flag) {
       // Let the copies already issued land before the CTA's shared memory
       // is released (bounded as well).
-      for (int kb = issued > NST ? issued - NST : 0; kb < issued; ++kb) {
+      for (int q = g > NST ? g - NST : 0; q < g; ++q) {
         const unsigned long long t0 = now_ns();
-        while (!mbar_test(&full[kb % NST], (kb / NST) & 1) && now_ns() - t0 < WAIT_NS) {
+        while (!mbar_test(&full[q % NST], (q / NST) & 1) && now_ns() - t0 < WAIT_NS) {
         }
       }
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer. Planes in a stage: A re_hi, re_lo, im_hi, im_lo, then B.
-    // Chunk c (CHUNK k-steps) accumulates from zero into TMEM buffer c % 2;
-    // the epilogue warps add it into their FP32 registers and free it.
+    // Chunk c (CHUNK k-steps of one tile; c counts across tiles) accumulates
+    // from zero into TMEM buffer c % 2; the epilogue warps add it into their
+    // FP32 registers and free it.
     const std::uint32_t idp = idesc_kind<KIND>(BM, BN, false), idn = idesc_kind<KIND>(BM, BN, true);
-    for (int kb = 0; kb < kblocks; ++kb) {
-      const int s = kb % NST;
-      const int c = kb / CHUNK, buf = c & 1;
-      const bool first = kb % CHUNK == 0;
-      if (first && c >= 2) {
-        // The epilogue's TMEM reads of this buffer precede the MMAs that
-        // overwrite it.
-        if (!mbar_wait(&acc_empty[buf], ((c >> 1) - 1) & 1, abort_flag, err, 4)) break;
-        asm volatile("tcgen05.fence::after_thread_sync;");
-      }
-      // Operand stages need no fence: the TMA's complete_tx on the barrier
-      // orders its shared-memory writes before the MMAs' reads.
-      if (!mbar_wait(&full[s], (kb / NST) & 1, abort_flag, err, 2)) break;
-      const std::uint32_t d_re = tmem + buf * 2 * BN, d_im = d_re + BN;
-      const std::uint32_t a0 = smem_u32(smem + s * SBYTES);
-      const std::uint32_t b0 = a0 + TILE_A;
-      const std::uint64_t arh = smem_desc_sw128(a0), arl = smem_desc_sw128(a0 + 32),
-                          aih = smem_desc_sw128(a0 + 64), ail = smem_desc_sw128(a0 + 96);
-      const std::uint64_t brh = smem_desc_sw128(b0), brl = smem_desc_sw128(b0 + 32),
-                          bih = smem_desc_sw128(b0 + 64), bil = smem_desc_sw128(b0 + 96);
-      const std::uint32_t acc = first ? 0u : 1u;
-      if constexpr (KIND == KIND_BF16) {
-        // Pieces 0 and 1 sit in the 128-byte rows (re0 re1 im0 im1, named
-        // *h and *l above), piece 2 in the 64-byte rows (re2 im2). Per real
-        // product x*y the terms x2y0, x1y1, x0y2 (~2^-16), x1y0, x0y1
-        // (~2^-8) and x0y0, smallest first.
-        const std::uint32_t at = a0 + 2 * TILE_A, bt = at + TAIL;
-        const std::uint64_t ar2 = smem_desc_sw64(at), ai2 = smem_desc_sw64(at + 32);
-        const std::uint64_t br2 = smem_desc_sw64(bt), bi2 = smem_desc_sw64(bt + 32);
-        // C_re = Ar Br - Ai Bi
-        umma<KIND>(d_re, ar2, brh, idp, acc);
-        umma<KIND>(d_re, arl, brl, idp, 1);
-        umma<KIND>(d_re, arh, br2, idp, 1);
-        umma<KIND>(d_re, ai2, bih, idn, 1);
-        umma<KIND>(d_re, ail, bil, idn, 1);
-        umma<KIND>(d_re, aih, bi2, idn, 1);
-        umma<KIND>(d_re, arl, brh, idp, 1);
-        umma<KIND>(d_re, arh, brl, idp, 1);
-        umma<KIND>(d_re, ail, bih, idn, 1);
-        umma<KIND>(d_re, aih, bil, idn, 1);
-        umma<KIND>(d_re, arh, brh, idp, 1);
-        umma<KIND>(d_re, aih, bih, idn, 1);
-        // C_im = Ar Bi + Ai Br
-        umma<KIND>(d_im, ar2, bih, idp, acc);
-        umma<KIND>(d_im, arl, bil, idp, 1);
-        umma<KIND>(d_im, arh, bi2, idp, 1);
-        umma<KIND>(d_im, ai2, brh, idp, 1);
-        umma<KIND>(d_im, ail, brl, idp, 1);
-        umma<KIND>(d_im, aih, br2, idp, 1);
-        umma<KIND>(d_im, arl, bih, idp, 1);
-        umma<KIND>(d_im, arh, bil, idp, 1);
-        umma<KIND>(d_im, ail, brh, idp, 1);
-        umma<KIND>(d_im, aih, brl, idp, 1);
-        umma<KIND>(d_im, arh, bih, idp, 1);
-        umma<KIND>(d_im, aih, brh, idp, 1);
+    int g = 0, c = 0;
+    bool go = true;
+    for (int t = blockIdx.x; t < total && go; t += gridDim.x) {
+      for (int kb = 0; kb < kblocks; ++kb, ++g) {
+        const int s = g % NST;
+        const int buf = c & 1;
+        const bool first = kb % CHUNK == 0;
+        if (first && c >= 2) {
+          // The epilogue's TMEM reads of this buffer precede the MMAs that
+          // overwrite it.
+          if (!mbar_wait(&acc_empty[buf], ((c >> 1) - 1) & 1, abort_flag, err, 4)) {
+            go = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+        }
+        // Operand stages need no fence: the TMA's complete_tx on the barrier
+        // orders its shared-memory writes before the MMAs' reads.
+        if (!mbar_wait(&full[s], (g / NST) & 1, abort_flag, err, 2)) {
+          go = false;
+          break;
+        }
+        const std::uint32_t d_re = tmem + buf * 2 * BN, d_im = d_re + BN;
+        const std::uint32_t a0 = smem_u32(smem + s * SBYTES);
+        const std::uint32_t b0 = a0 + TILE_A;
+        const std::uint64_t arh = smem_desc_sw128(a0), arl = smem_desc_sw128(a0 + 32),
+                            aih = smem_desc_sw128(a0 + 64), ail = smem_desc_sw128(a0 + 96);
+        const std::uint64_t brh = smem_desc_sw128(b0), brl = smem_desc_sw128(b0 + 32),
+                            bih = smem_desc_sw128(b0 + 64), bil = smem_desc_sw128(b0 + 96);
+        const std::uint32_t acc = first ? 0u : 1u;
+        if constexpr (KIND == KIND_BF16) {
+          // Pieces 0 and 1 sit in the 128-byte rows (re0 re1 im0 im1, named
+          // *h and *l above), piece 2 in the 64-byte rows (re2 im2). Per real
+          // product x*y the terms x2y0, x1y1, x0y2 (~2^-16), x1y0, x0y1
+          // (~2^-8) and x0y0, smallest first.
+          const std::uint32_t at = a0 + 2 * TILE_A, bt = at + TAIL;
+          const std::uint64_t ar2 = smem_desc_sw64(at), ai2 = smem_desc_sw64(at + 32);
+          const std::uint64_t br2 = smem_desc_sw64(bt), bi2 = smem_desc_sw64(bt + 32);
+          // C_re = Ar Br - Ai Bi
+          umma<KIND>(d_re, ar2, brh, idp, acc);
+          umma<KIND>(d_re, arl, brl, idp, 1);
+          umma<KIND>(d_re, arh, br2, idp, 1);
+          umma<KIND>(d_re, ai2, bih, idn, 1);
+          umma<KIND>(d_re, ail, bil, idn, 1);
+          umma<KIND>(d_re, aih, bi2, idn, 1);
+          umma<KIND>(d_re, arl, brh, idp, 1);
+          umma<KIND>(d_re, arh, brl, idp, 1);
+          umma<KIND>(d_re, ail, bih, idn, 1);
+          umma<KIND>(d_re, aih, bil, idn, 1);
+          umma<KIND>(d_re, arh, brh, idp, 1);
+          umma<KIND>(d_re, aih, bih, idn, 1);
+          // C_im = Ar Bi + Ai Br
+          umma<KIND>(d_im, ar2, bih, idp, acc);
+          umma<KIND>(d_im, arl, bil, idp, 1);
+          umma<KIND>(d_im, arh, bi2, idp, 1);
+          umma<KIND>(d_im, ai2, brh, idp, 1);
+          umma<KIND>(d_im, ail, brl, idp, 1);
+          umma<KIND>(d_im, aih, br2, idp, 1);
+          umma<KIND>(d_im, arl, bih, idp, 1);
+          umma<KIND>(d_im, arh, bil, idp, 1);
+          umma<KIND>(d_im, ail, brh, idp, 1);
+          umma<KIND>(d_im, aih, brl, idp, 1);
+          umma<KIND>(d_im, arh, bih, idp, 1);
+          umma<KIND>(d_im, aih, brh, idp, 1);
+        } else {
+          // The small hi*lo terms go first and the two large hi*hi terms
+          // last, so only those two additions round against a large
+          // accumulator.
+          umma<KIND>(d_re, arh, brl, idp, acc);
+          umma<KIND>(d_re, arl, brh, idp, 1);
+          umma<KIND>(d_re, aih, bil, idn, 1);
+          umma<KIND>(d_re, ail, bih, idn, 1);
+          umma<KIND>(d_re, arh, brh, idp, 1);
+          umma<KIND>(d_re, aih, bih, idn, 1);
+          umma<KIND>(d_im, arh, bil, idp, acc);
+          umma<KIND>(d_im, arl, bih, idp, 1);
+          umma<KIND>(d_im, aih, brl, idp, 1);
+          umma<KIND>(d_im, ail, brh, idp, 1);
+          umma<KIND>(d_im, arh, bih, idp, 1);
+          umma<KIND>(d_im, aih, brh, idp, 1);
+        }
         umma_commit(&empty[s]);
-        if (kb % CHUNK == CHUNK - 1 || kb == kblocks - 1) umma_commit(&acc_full[buf]);
-        continue;
+        if (kb % CHUNK == CHUNK - 1 || kb == kblocks - 1) {
+          umma_commit(&acc_full[buf]);
+          ++c;
+        }
       }
-      // The small hi*lo terms go first and the two large hi*hi terms last,
-      // so only those two additions round against a large accumulator.
-      umma<KIND>(d_re, arh, brl, idp, acc);
-      umma<KIND>(d_re, arl, brh, idp, 1);
-      umma<KIND>(d_re, aih, bil, idn, 1);
-      umma<KIND>(d_re, ail, bih, idn, 1);
-      umma<KIND>(d_re, arh, brh, idp, 1);
-      umma<KIND>(d_re, aih, bih, idn, 1);
-      umma<KIND>(d_im, arh, bil, idp, acc);
-      umma<KIND>(d_im, arl, bih, idp, 1);
-      umma<KIND>(d_im, aih, brl, idp, 1);
-      umma<KIND>(d_im, ail, brh, idp, 1);
-      umma<KIND>(d_im, arh, bih, idp, 1);
-      umma<KIND>(d_im, aih, brh, idp, 1);
-      umma_commit(&empty[s]);
-      if (kb % CHUNK == CHUNK - 1 || kb == kblocks - 1) umma_commit(&acc_full[buf]);
     }
     umma_commit(mma_done);
   } else if (warp >= 2) {
@@ -385,67 +410,71 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     const int q = warp % 4;
     const int half = (warp - 2) / 4;
     const int row = q * 32 + lane;
-    float tre[BN / 2], tim[BN / 2];
-#pragma unroll
-    for (int j = 0; j < BN / 2; ++j) tre[j] = tim[j] = 0.f;
+    float2* stg = staging + (warp - 2) * 32 * 32;
+    int c = 0;
     bool ok = true;
-    for (int c = 0; c < chunks; ++c) {
-      const int buf = c & 1;
-      if (!mbar_wait(&acc_full[buf], (c >> 1) & 1, abort_flag, err, 3)) {
-        ok = false;
-        break;
+    for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
+      int m0, n0, batch;
+      tile_of(t, m0, n0, batch);
+      float tre[BN / 2], tim[BN / 2];
+#pragma unroll
+      for (int j = 0; j < BN / 2; ++j) tre[j] = tim[j] = 0.f;
+      for (int cc = 0; cc < chunks; ++cc, ++c) {
+        const int buf = c & 1;
+        if (!mbar_wait(&acc_full[buf], (c >> 1) & 1, abort_flag, err, 3)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const std::uint32_t base = tmem + (std::uint32_t(q * 32) << 16) + buf * 2 * BN + half * (BN / 2);
+#pragma unroll
+        for (int j0 = 0; j0 < BN / 2; j0 += 32) {
+          // Both loads in flight before one wait: two TMEM round trips per
+          // chunk instead of four.
+          std::uint32_t vr[32], vi[32];
+          TMEM_LD32(base + j0, vr);
+          TMEM_LD32(base + BN + j0, vi);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            tre[j0 + j] += __uint_as_float(vr[j]);
+            tim[j0 + j] += __uint_as_float(vi[j]);
+          }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty[buf]);
       }
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      const std::uint32_t base = tmem + (std::uint32_t(q * 32) << 16) + buf * 2 * BN + half * (BN / 2);
+      if (!ok) break;
+      // The MMA issuer already works on the next tile. The warp's 32 x 64
+      // block leaves through its staging area as whole 32-column row pieces:
+      // element (r, j) of a 32 x 32 piece sits at r * 32 + (j ^ r).
+      const int ncols = n - n0 - half * (BN / 2);
+      int ea = 0;
+      const int* eb = nullptr;
+      if (KIND == KIND_FP16) {
+        ea = m0 + row < m ? exp_a[std::uint64_t(batch) * m + m0 + row] : 0;
+        eb = exp_b + std::uint64_t(batch) * n + n0 + half * (BN / 2);
+      }
+      float2* cb = C + std::uint64_t(batch) * c_batch_stride;
 #pragma unroll
       for (int j0 = 0; j0 < BN / 2; j0 += 32) {
-        // Both loads in flight before one wait: two TMEM round trips per
-        // chunk instead of four.
-        std::uint32_t vr[32], vi[32];
-        TMEM_LD32(base + j0, vr);
-        TMEM_LD32(base + BN + j0, vi);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
-          tre[j0 + j] += __uint_as_float(vr[j]);
-          tim[j0 + j] += __uint_as_float(vi[j]);
+          float2 v = make_float2(tre[j0 + j], tim[j0 + j]);
+          if (KIND == KIND_FP16) {
+            const int e = j0 + j < ncols ? -(ea + eb[j0 + j]) : 0;
+            v = make_float2(ldexpf(v.x, e), ldexpf(v.y, e));
+          }
+          stg[lane * 32 + (j ^ lane)] = v;
         }
-      }
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&acc_empty[buf]);
-    }
-    // The tile goes out through shared memory so that the global stores
-    // are whole rows: once the last chunk is complete every MMA has read
-    // its operand stages, so they are free. Row stride BN + 1 keeps the
-    // column writes at most 2-way bank conflicted.
-    float2* stile = reinterpret_cast<float2*>(smem);
-    const int ncols = n - n0 - half * (BN / 2);
-    if (ok) {
-      float2* srow = stile + row * (BN + 1) + half * (BN / 2);
-      if (KIND == KIND_FP16) {
-        // Undo the row scales of A (this row) and B (each column).
-        const int ea = m0 + row < m ? exp_a[std::uint64_t(batch) * m + m0 + row] : 0;
-        const int* eb = exp_b + std::uint64_t(batch) * n + n0 + half * (BN / 2);
-#pragma unroll
-        for (int j = 0; j < BN / 2; ++j) {
-          const int e = j < ncols ? -(ea + eb[j]) : 0;
-          srow[j] = make_float2(ldexpf(tre[j], e), ldexpf(tim[j], e));
+        __syncwarp();
+        for (int r = 0; r < 32; ++r) {
+          const int gr = m0 + q * 32 + r;
+          if (gr < m && j0 + lane < ncols)
+            cb[std::uint64_t(gr) * n + n0 + half * (BN / 2) + j0 + lane] = stg[r * 32 + (lane ^ r)];
         }
-      } else {
-#pragma unroll
-        for (int j = 0; j < BN / 2; ++j) srow[j] = make_float2(tre[j], tim[j]);
-      }
-    }
-    asm volatile("bar.sync 1, %0;" ::"r"(32 * EPI_WARPS) : "memory");  // the epilogue warps only
-    if (!*abort_flag) {
-      const int ew = warp - 2;
-      float2* cb = C + std::uint64_t(batch) * c_batch_stride;
-      const int rows = min(BM, m - m0), cols = min(BN, n - n0);
-      for (int r = ew; r < rows; r += EPI_WARPS) {
-        float2* crow = cb + std::uint64_t(m0 + r) * n + n0;
-        const float2* srow = stile + r * (BN + 1);
-        for (int c = lane; c < cols; c += 32) crow[c] = srow[c];
+        __syncwarp();
       }
     }
   }
@@ -464,28 +493,28 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
 
 __global__ void __launch_bounds__(THREADS, 1)
     cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
-                        float2* __restrict__ C, int m, int n, int k, std::uint64_t c_batch_stride,
+                        float2* __restrict__ C, int m, int n, int k, int batches, std::uint64_t c_batch_stride,
                         int* __restrict__ err, int CHUNK) {
-  cgemm_split_body<KIND_TF32>(&map_a, &map_b, nullptr, nullptr, C, m, n, k, c_batch_stride, err, CHUNK, nullptr,
-                              nullptr);
+  cgemm_split_body<KIND_TF32>(&map_a, &map_b, nullptr, nullptr, C, m, n, k, batches, c_batch_stride, err, CHUNK,
+                              nullptr, nullptr);
 }
 
 __global__ void __launch_bounds__(THREADS, 1)
     cgemm_fp16x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
-                        float2* __restrict__ C, int m, int n, int k, std::uint64_t c_batch_stride,
+                        float2* __restrict__ C, int m, int n, int k, int batches, std::uint64_t c_batch_stride,
                         int* __restrict__ err, int CHUNK, const int* __restrict__ exp_a,
                         const int* __restrict__ exp_b) {
-  cgemm_split_body<KIND_FP16>(&map_a, &map_b, nullptr, nullptr, C, m, n, k, c_batch_stride, err, CHUNK, exp_a,
-                              exp_b);
+  cgemm_split_body<KIND_FP16>(&map_a, &map_b, nullptr, nullptr, C, m, n, k, batches, c_batch_stride, err, CHUNK,
+                              exp_a, exp_b);
 }
 
 __global__ void __launch_bounds__(THREADS, 1)
     cgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                         const __grid_constant__ CUtensorMap map_a2, const __grid_constant__ CUtensorMap map_b2,
-                        float2* __restrict__ C, int m, int n, int k, std::uint64_t c_batch_stride,
+                        float2* __restrict__ C, int m, int n, int k, int batches, std::uint64_t c_batch_stride,
                         int* __restrict__ err, int CHUNK) {
-  cgemm_split_body<KIND_BF16>(&map_a, &map_b, &map_a2, &map_b2, C, m, n, k, c_batch_stride, err, CHUNK, nullptr,
-                              nullptr);
+  cgemm_split_body<KIND_BF16>(&map_a, &map_b, &map_a2, &map_b2, C, m, n, k, batches, c_batch_stride, err, CHUNK,
+                              nullptr, nullptr);
 }
 
 // ---- CTA-pair kernel (cta_group::2) -------------------------------------------
@@ -998,6 +1027,21 @@ std::size_t tc_workspace_elems(std::size_t m, std::size_t n, std::size_t k) {
   return tf32 > fp16 ? tf32 : fp16;
 }
 
+// Grid of the persistent single-CTA kernels: one CTA per SM (at most one
+// per tile); QFLEX_TC_PERSIST=0 launches one CTA per tile instead.
+unsigned persistent_grid(std::size_t tiles) {
+  static const int sms = [] {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess)
+      v = 152;
+    const char* e = std::getenv("QFLEX_TC_PERSIST");
+    if (e && std::atoi(e) == 0) v = 0;
+    return v;
+  }();
+  return (unsigned)(sms > 0 ? std::min<std::size_t>(tiles, (std::size_t)sms) : tiles);
+}
+
 TcConfig tc_default_config() {
   TcConfig c;
   // k-steps per TMEM chunk. Measured on the 7x7 (1+32+1) network (8
@@ -1053,8 +1097,8 @@ void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size
   const CUtensorMap ma = plane_map(pa, m, kpad, batch, BM);
   const CUtensorMap mb = plane_map(pb, n, kpad, batch, BN);
   const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
-  dim3 grid((unsigned)tiles, 1, (unsigned)batch);
-  cgemm_tf32x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err,
+  dim3 grid(persistent_grid(tiles * (std::size_t)batch), 1, 1);
+  cgemm_tf32x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch, batch_stride, err,
                                                         chunk);
   check(cudaGetLastError(), "cgemm_tf32x3");
 }
@@ -1085,8 +1129,8 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
   const CUtensorMap ma = plane_map_f16(pa, m, kpad, batch, BM);
   const CUtensorMap mb = plane_map_f16(pb, n, kpad, batch, BN);
   const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
-  dim3 grid((unsigned)tiles, 1, (unsigned)batch);
-  cgemm_fp16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch_stride, err,
+  dim3 grid(persistent_grid(tiles * (std::size_t)batch), 1, 1);
+  cgemm_fp16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch, batch_stride, err,
                                                         cfg.chunk, ea, eb);
   check(cudaGetLastError(), "cgemm_fp16x3");
 }
@@ -1120,8 +1164,8 @@ void launch_cgemm_bf16x3(const float2* A, const float2* Bt, float2* C, std::size
   const CUtensorMap ma2 = plane_map_bf16(at, m, kpad, batch, BM, 32);
   const CUtensorMap mb2 = plane_map_bf16(bt, n, kpad, batch, BN, 32);
   const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
-  dim3 grid((unsigned)tiles, 1, (unsigned)batch);
-  cgemm_bf16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, ma2, mb2, C, (int)m, (int)n, (int)k, batch_stride,
+  dim3 grid(persistent_grid(tiles * (std::size_t)batch), 1, 1);
+  cgemm_bf16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, ma2, mb2, C, (int)m, (int)n, (int)k, batch, batch_stride,
                                                         err, cfg.chunk);
   check(cudaGetLastError(), "cgemm_bf16x3");
 }
