@@ -129,6 +129,11 @@ size_t qflex_gb300_last_ops(const qflex_gb300_context* ctx, double* out, size_t 
  *                replay it (default 1, or QFLEX_GB300_GRAPHS)
  *   "max_batch"  most output strings per device pass of evaluate_many
  *                (0: as many as fit in device memory; default 0)
+ *   "fuse_splits" 1 (3xFP16): a permutation whose output is the next
+ *                product's A operand and read by nothing else writes the FP16
+ *                planes (scaled per 32 values of a row) directly instead of
+ *                complex64, and the product skips splitting A (default 1,
+ *                or QFLEX_GB300_FUSE)
  *   "open_terminals" 1: terminal cuts that take all their values, with no
  *                two-qubit cut after them, stay open indices -- the ops after
  *                them run once on tensors carrying the open indices instead

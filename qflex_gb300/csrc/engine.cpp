@@ -48,6 +48,12 @@ struct Engine::Plan {
   Network net;
   Program prog;
   std::vector<PermPlan> perm;  // indexed like prog.ops (unused for GEMM ops)
+  // 3xFP16 fusion, indexed like prog.ops: a permute that writes the next
+  // product's A operand straight as FP16 planes has fused[i] = index of that
+  // product; the product has fused[j] = j. -1 elsewhere. Recomputed when
+  // the options change (fuse_version).
+  std::vector<int> fused;
+  unsigned fuse_version = ~0u;
   int precision = -1;          // precision the program was planned for
   std::size_t tc_ws_elems = 0; // split-plane workspace of one batch entry
   std::uint32_t max_size_log2 = 0;
@@ -84,6 +90,7 @@ Engine::Engine(int device, int precision) : device_(device), precision_(precisio
   QFX_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
   own_stream_ = true;
   if (const char* g = std::getenv("QFLEX_GB300_GRAPHS")) graphs_ = std::atoi(g) != 0;
+  if (const char* f = std::getenv("QFLEX_GB300_FUSE")) fuse_splits_ = std::atoi(f) != 0;
   QFX_CUDA(cudaEventCreate(&ev0_));
   QFX_CUDA(cudaEventCreate(&ev1_));
   set_precision(precision);
@@ -118,6 +125,9 @@ void Engine::set_option(const std::string& name, double value) {
   } else if (name == "graphs") {
     if (value != 0 && value != 1) throw QFX_ERR("Option graphs must be 0 or 1.");
     graphs_ = value != 0;
+  } else if (name == "fuse_splits") {
+    if (value != 0 && value != 1) throw QFX_ERR("Option fuse_splits must be 0 or 1.");
+    fuse_splits_ = value != 0;
   } else if (name == "open_terminals") {
     if (value != 0 && value != 1) throw QFX_ERR("Option open_terminals must be 0 or 1.");
     open_terminals_ = value != 0;
@@ -137,6 +147,7 @@ double Engine::get_option(const std::string& name) const {
   if (name == "graphs") return graphs_ ? 1 : 0;
   if (name == "max_batch") return max_batch_;
   if (name == "open_terminals") return open_terminals_ ? 1 : 0;
+  if (name == "fuse_splits") return fuse_splits_ ? 1 : 0;
   throw QFX_ERR("Unknown option '", name, "'.");
 }
 
@@ -337,6 +348,59 @@ T* upload(const std::vector<T>& v) {
 
 }  // namespace
 
+namespace {
+
+bool overlaps(std::size_t a0, std::size_t a1, std::size_t b0, std::size_t b1) { return a0 < b1 && b0 < a1; }
+
+// Whether the output of permute i, the A operand of product j, is read by no
+// other op before it is overwritten or the program ends.
+bool only_read_by(const std::vector<DevOp>& ops, std::size_t i, std::size_t j) {
+  const std::size_t c0 = ops[i].c, c1 = c0 + (std::size_t(1) << ops[i].nbits);
+  for (std::size_t q = i + 1; q < ops.size(); ++q) {
+    const DevOp& op = ops[q];
+    std::size_t w0, w1;
+    if (op.kind == DevOp::PERMUTE) {
+      const std::size_t sz = std::size_t(1) << op.nbits;
+      if (overlaps(op.a, op.a + sz, c0, c1)) return false;
+      w0 = op.c;
+      w1 = op.c + sz;
+    } else {
+      if (q != j && overlaps(op.a, op.a + op.m * op.k, c0, c1)) return false;
+      if (overlaps(op.b, op.b + op.k * op.n, c0, c1)) return false;
+      w0 = op.c;
+      w1 = op.c + op.m * op.n;
+    }
+    if (w0 <= c0 && c1 <= w1) return true;  // overwritten whole
+  }
+  return true;
+}
+
+}  // namespace
+
+void Engine::plan_fusion(Plan& p) {
+  const auto& ops = p.prog.ops;
+  p.fused.assign(ops.size(), -1);
+  p.fuse_version = options_version_;
+  if (precision_ != FP16X3 || !fuse_splits_) return;
+  for (std::size_t i = 0; i < ops.size(); ++i) {
+    if (ops[i].kind != DevOp::PERMUTE) continue;
+    // The product that reads it as A: the next op, or the one after a
+    // permute of its B operand.
+    for (std::size_t j = i + 1; j < ops.size() && j <= i + 2; ++j) {
+      const DevOp& g = ops[j];
+      if (g.kind == DevOp::PERMUTE) continue;
+      if (!g.b_nk || g.a != ops[i].c || g.m * g.k != (std::size_t(1) << ops[i].nbits)) break;
+      const TcConfig cfg = tc_config(g.m, g.n, g.k);
+      if (g.k < 32 || (g.k & (g.k - 1)) != 0 || cfg.chunk > 2) break;
+      if (only_read_by(ops, i, j)) {
+        p.fused[i] = (int)j;
+        p.fused[j] = (int)j;
+      }
+      break;
+    }
+  }
+}
+
 std::size_t Engine::run_program(Plan& p, int batch, float2* arena, float* tc_ws) {
   const Program& prog = p.prog;
   std::size_t launches = 0;
@@ -350,16 +414,32 @@ std::size_t Engine::run_program(Plan& p, int batch, float2* arena, float* tc_ws)
       prof_events_.push_back(e);
     }
   }
+  if (p.fuse_version != options_version_ || p.fused.size() != prog.ops.size()) plan_fusion(p);
   for (std::size_t i = 0; i < prog.ops.size(); ++i) {
     const DevOp& op = prog.ops[i];
     if (profile_) QFX_CUDA(cudaEventRecord(prof_events_[i], stream_));
     if (op.kind == DevOp::PERMUTE) {
-      launch_permute(p.perm[i], arena + op.a, arena + op.c, stride, batch, stream_);
+      if (p.fused[i] >= 0) {
+        // Straight into the A planes of the product that follows.
+        const DevOp& g = prog.ops[p.fused[i]];
+        const Fp16Workspace w = fp16_workspace(tc_ws, g.m, g.n, g.k, batch);
+        int kl = 0;
+        while ((std::size_t(1) << kl) < g.k) ++kl;
+        launch_permute_fp16_planes(p.perm[i], arena + op.a, stride, w.a_planes, w.a_block_exps, g.m, kl, batch,
+                                   stream_);
+      } else {
+        launch_permute(p.perm[i], arena + op.a, arena + op.c, stride, batch, stream_);
+      }
       launches += 1;
     } else if (op.b_nk) {
-      launch_split_product(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, stride, batch,
-                           tc_ws);
-      launches += 3;  // two plane splits and the product
+      const bool a_planes = p.fused[i] == (int)i;
+      if (a_planes)
+        launch_cgemm_fp16x3(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, stride, batch,
+                            tc_ws, error_flag(), tc_config(op.m, op.n, op.k), stream_, true);
+      else
+        launch_split_product(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, stride, batch,
+                             tc_ws);
+      launches += a_planes ? 2 : 3;  // plane splits and the product
     } else {
       launch_cgemm_fp32(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, batch,
                         stream_, scratch);

@@ -104,6 +104,8 @@ class Engine {
   struct Plan;
   Plan* get_plan(const std::string& circuit, const std::string& ordering, const std::string& grid);
   std::size_t run_program(Plan& p, int batch, float2* arena, float* tc_ws);
+  // Marks permute/product pairs whose A operand goes straight into planes.
+  void plan_fusion(Plan& p);
 
   int device_;
   int precision_;
@@ -115,6 +117,7 @@ class Engine {
   std::map<std::tuple<std::size_t, std::size_t, std::size_t>, int> tc_variant_;
   int max_batch_ = 0;            // output strings per device pass (0: as many as fit)
   bool open_terminals_ = true;   // terminal cuts as open indices where the planner can
+  bool fuse_splits_ = true;      // 3xFP16: permutes write the next product's A planes
   unsigned options_version_ = 0;  // part of the graph key: options change launches
   TcConfig tc_config(std::size_t m, std::size_t n, std::size_t k) const;
   // C = A * Bt^T on the tensor cores in the context's split precision.

@@ -6,6 +6,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_fp16.h>
+
 #include "kernels.h"
 
 namespace qfx {
@@ -127,10 +129,20 @@ __global__ void __launch_bounds__(256) flatten_kernel(const ColumnDesc* __restri
 // ---------------------------------------------------------------------------
 // Binary-digit permutation.
 // ---------------------------------------------------------------------------
+// Output of the FP16-plane form of the permutation (see
+// launch_permute_fp16_planes).
+struct PlaneOut {
+  __half* planes;
+  int* exps;
+  std::uint64_t rows;
+  std::uint32_t k_log2;
+};
+
+template <bool PLANES>
 __global__ void __launch_bounds__(256) permute_kernel(const __grid_constant__ PermPlan P,
                                                       const float2* __restrict__ src,
                                                       float2* __restrict__ dst,
-                                                      std::uint64_t batch_stride) {
+                                                      std::uint64_t batch_stride, PlaneOut po) {
   __shared__ float2 tile[1024];
   __shared__ std::uint32_t tab[6 * 32];
   if (threadIdx.x < 6 * 32) tab[threadIdx.x] = P.tab[threadIdx.x / 32][threadIdx.x % 32];
@@ -165,7 +177,36 @@ __global__ void __launch_bounds__(256) permute_kernel(const __grid_constant__ Pe
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const std::uint32_t j = threadIdx.x + 256u * i;
-      if (j < T) d[bo + tab[64 + (j & 31)] + tab[96 + (j >> 5)]] = tile[perm_swizzle(tab[128 + (j & 31)] + tab[160 + (j >> 5)])];
+      if (j >= T) continue;  // T is a multiple of 32 here: whole warps
+      const std::uint64_t o = bo + tab[64 + (j & 31)] + tab[96 + (j >> 5)];
+      const float2 v = tile[perm_swizzle(tab[128 + (j & 31)] + tab[160 + (j >> 5)])];
+      if (!PLANES) {
+        d[o] = v;
+        continue;
+      }
+      // The warp's 32 values are outputs o - lane .. o - lane + 31: one
+      // 32-aligned run of a row (the tile holds the 5 lowest output digits).
+      float mx = fmaxf(fabsf(v.x), fabsf(v.y));
+#pragma unroll
+      for (int w = 16; w; w >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, w));
+      int e = 0;
+      if (mx > 0.f && isfinite(mx)) {
+        int ex;
+        frexpf(mx, &ex);  // mx in [2^(ex-1), 2^ex)
+        e = 15 - ex;
+      }
+      const std::uint64_t k = std::uint64_t(1) << po.k_log2;
+      const std::uint64_t row = o >> po.k_log2, kk = o & (k - 1);
+      const float xr = ldexpf(v.x, e), xi = ldexpf(v.y, e);
+      const __half rh = __float2half_rn(xr), ih = __float2half_rn(xi);
+      __half* pl = po.planes + std::uint64_t(blockIdx.y) * 4 * po.rows * k + ((kk / 16) * po.rows + row) * 64 +
+                   (kk % 16);
+      pl[0] = rh;
+      pl[16] = __float2half_rn(xr - __half2float(rh));
+      pl[32] = ih;
+      pl[48] = __float2half_rn(xi - __half2float(ih));
+      if ((threadIdx.x & 31) == 0)
+        po.exps[std::uint64_t(blockIdx.y) * po.rows * (k / 32) + row * (k / 32) + kk / 32] = e;
     }
     __syncthreads();
   }
@@ -587,8 +628,21 @@ void launch_permute(const PermPlan& plan, const float2* src, float2* dst, std::u
   const std::uint64_t tiles = plan.n_tiles;
   const unsigned gx = (unsigned)std::min<std::uint64_t>(tiles, 152ull * 16ull);
   dim3 grid(gx, (unsigned)batch, 1);
-  permute_kernel<<<grid, 256, 0, s>>>(plan, src, dst, batch_stride);
+  permute_kernel<false><<<grid, 256, 0, s>>>(plan, src, dst, batch_stride, PlaneOut{});
   check_launch("permute");
+}
+
+void launch_permute_fp16_planes(const PermPlan& plan, const float2* src, std::uint64_t src_batch_stride,
+                                void* planes, int* exps, std::uint64_t rows, int k_log2, int batch,
+                                cudaStream_t s) {
+  if (k_log2 < 5 || plan.tile_bits < 5)
+    throw std::string("ERROR (qflex_gb300: permute) --> plane output needs rows of at least 32 values");
+  const std::uint64_t tiles = plan.n_tiles;
+  const unsigned gx = (unsigned)std::min<std::uint64_t>(tiles, 152ull * 16ull);
+  dim3 grid(gx, (unsigned)batch, 1);
+  permute_kernel<true><<<grid, 256, 0, s>>>(plan, src, nullptr, src_batch_stride,
+                                            PlaneOut{static_cast<__half*>(planes), exps, rows, (std::uint32_t)k_log2});
+  check_launch("permute_fp16_planes");
 }
 
 int vm_splits(std::size_t m, std::size_t n, std::size_t k, int batch) {

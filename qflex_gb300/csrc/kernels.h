@@ -78,6 +78,16 @@ void permute_schedule_on_host(const PermPlan& plan, const float2* src, float2* d
                               std::uint64_t size);
 void launch_permute(const PermPlan& plan, const float2* src, float2* dst, std::uint64_t batch_stride,
                     int batch, cudaStream_t s);
+// The same permutation writing its output, a row-major [rows][k] operand
+// (k a power of two >= 32), as the 3xFP16 tensor-core planes instead of
+// complex64: [k / 16][rows][plane 4][16] fp16 per batch entry (the layout
+// the product kernel loads), every 32 consecutive values of a row scaled by
+// their own power of two 2^e (max in [2^14, 2^15)), e stored at
+// exps[row * (k / 32) + kk / 32]. Planes of batch entry b start at
+// planes + b * 4 * rows * k, exponents at exps + b * rows * (k / 32).
+void launch_permute_fp16_planes(const PermPlan& plan, const float2* src, std::uint64_t src_batch_stride,
+                                void* planes, int* exps, std::uint64_t rows, int k_log2, int batch,
+                                cudaStream_t s);
 
 // ---- complex64 products on CUDA cores -------------------------------------------
 // C[m,n] = A[m,k] * B[k,n], row-major, all three advanced by batch_stride

@@ -208,8 +208,11 @@ __device__ __forceinline__ void mbar_arrive(std::uint64_t* bar) {
 // b + gridDim.x, ... (grouped raster, batch entries after each other), and
 // its producer, MMA issuer and epilogue run through the tiles on shared
 // stage and chunk counters, so one tile's epilogue overlaps the next tile's
-// loads and MMAs. KIND_FP16 operands carry per-row scale exponents (value =
-// plane value * 2^-e); the epilogue removes them. KIND_BF16 operands have
+// loads and MMAs. KIND_FP16 operands carry power-of-two scale exponents
+// (value = plane value * 2^-e) per row, or for A with a_blocks > 0 per 32
+// values of a row (a_blocks = k / 32 per row; then every TMEM chunk, which
+// lies inside one block, is scaled as it is added); the epilogue removes
+// them. KIND_BF16 operands have
 // six planes per k-step: b0, b1 of re and im in a 128-byte row (map_a /
 // map_b) and b2 of re and im in a 64-byte row (map_a2 / map_b2).
 template <int KIND>
@@ -218,7 +221,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
                                                  float2* __restrict__ C, int m, int n, int k, int batches,
                                                  std::uint64_t c_batch_stride, int* __restrict__ err, int CHUNK,
                                                  const int* __restrict__ exp_a,
-                                                 const int* __restrict__ exp_b) {
+                                                 const int* __restrict__ exp_b, int a_blocks) {
   constexpr int KSTEP = KIND == KIND_TF32 ? 8 : 16;  // k values per plane row of 32 bytes
   constexpr int TAIL = BM * 64;                       // BF16 third-piece tile of one operand
   constexpr int NST = KIND == KIND_BF16 ? 3 : STAGES;
@@ -426,6 +429,13 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
+        // Scale of this chunk: 1, or 2^-e of A's block for this row.
+        float sa = 1.f;
+        if (KIND == KIND_FP16 && a_blocks > 0) {
+          const int blk = (cc * CHUNK * KSTEP) / 32;
+          const int e = m0 + row < m ? exp_a[(std::uint64_t(batch) * m + m0 + row) * a_blocks + blk] : 0;
+          sa = ldexpf(1.f, -e);
+        }
         const std::uint32_t base = tmem + (std::uint32_t(q * 32) << 16) + buf * 2 * BN + half * (BN / 2);
 #pragma unroll
         for (int j0 = 0; j0 < BN / 2; j0 += 32) {
@@ -437,8 +447,8 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
-            tre[j0 + j] += __uint_as_float(vr[j]);
-            tim[j0 + j] += __uint_as_float(vi[j]);
+            tre[j0 + j] = fmaf(__uint_as_float(vr[j]), sa, tre[j0 + j]);
+            tim[j0 + j] = fmaf(__uint_as_float(vi[j]), sa, tim[j0 + j]);
           }
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
@@ -453,7 +463,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
       int ea = 0;
       const int* eb = nullptr;
       if (KIND == KIND_FP16) {
-        ea = m0 + row < m ? exp_a[std::uint64_t(batch) * m + m0 + row] : 0;
+        ea = (a_blocks == 0 && m0 + row < m) ? exp_a[std::uint64_t(batch) * m + m0 + row] : 0;
         eb = exp_b + std::uint64_t(batch) * n + n0 + half * (BN / 2);
       }
       float2* cb = C + std::uint64_t(batch) * c_batch_stride;
@@ -496,16 +506,16 @@ __global__ void __launch_bounds__(THREADS, 1)
                         float2* __restrict__ C, int m, int n, int k, int batches, std::uint64_t c_batch_stride,
                         int* __restrict__ err, int CHUNK) {
   cgemm_split_body<KIND_TF32>(&map_a, &map_b, nullptr, nullptr, C, m, n, k, batches, c_batch_stride, err, CHUNK,
-                              nullptr, nullptr);
+                              nullptr, nullptr, 0);
 }
 
 __global__ void __launch_bounds__(THREADS, 1)
     cgemm_fp16x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                         float2* __restrict__ C, int m, int n, int k, int batches, std::uint64_t c_batch_stride,
                         int* __restrict__ err, int CHUNK, const int* __restrict__ exp_a,
-                        const int* __restrict__ exp_b) {
+                        const int* __restrict__ exp_b, int a_blocks) {
   cgemm_split_body<KIND_FP16>(&map_a, &map_b, nullptr, nullptr, C, m, n, k, batches, c_batch_stride, err, CHUNK,
-                              exp_a, exp_b);
+                              exp_a, exp_b, a_blocks);
 }
 
 __global__ void __launch_bounds__(THREADS, 1)
@@ -514,7 +524,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                         float2* __restrict__ C, int m, int n, int k, int batches, std::uint64_t c_batch_stride,
                         int* __restrict__ err, int CHUNK) {
   cgemm_split_body<KIND_BF16>(&map_a, &map_b, &map_a2, &map_b2, C, m, n, k, batches, c_batch_stride, err, CHUNK,
-                              nullptr, nullptr);
+                              nullptr, nullptr, 0);
 }
 
 // ---- CTA-pair kernel (cta_group::2) -------------------------------------------
@@ -1023,7 +1033,7 @@ std::size_t tc_workspace_elems(std::size_t m, std::size_t n, std::size_t k) {
   // planes (4 fp16 per element) plus their row exponents and the BF16x3
   // planes (6 bf16 per element, fewer than the 3xTF32 ones).
   const std::size_t tf32 = 4 * (m + n) * ((k + 7) / 8 * 8);
-  const std::size_t fp16 = 2 * (m + n) * ((k + 15) / 16 * 16) + (m + n);
+  const std::size_t fp16 = 2 * (m + n) * ((k + 15) / 16 * 16) + (m + n) + m * ((k + 31) / 32) + 64;
   return tf32 > fp16 ? tf32 : fp16;
 }
 
@@ -1103,25 +1113,43 @@ void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size
   check(cudaGetLastError(), "cgemm_tf32x3");
 }
 
+Fp16Workspace fp16_workspace(float* workspace, std::size_t m, std::size_t n, std::size_t k, int batch) {
+  const std::size_t kpad = (k + 15) / 16 * 16, nb = (std::size_t)batch;
+  Fp16Workspace w;
+  __half* pa = reinterpret_cast<__half*>(workspace);
+  __half* pb = pa + 4 * m * kpad * nb;
+  w.a_planes = pa;
+  w.b_planes = pb;
+  w.a_exps = reinterpret_cast<int*>(pb + 4 * n * kpad * nb);
+  w.b_exps = w.a_exps + m * nb;
+  w.a_block_exps = w.b_exps + n * nb;
+  return w;
+}
+
 void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size_t m, std::size_t n,
                          std::size_t k, std::uint64_t batch_stride, std::uint64_t bt_stride, int batch,
-                         float* workspace, int* err, const TcConfig& cfg, cudaStream_t s) {
+                         float* workspace, int* err, const TcConfig& cfg, cudaStream_t s, bool a_in_planes) {
   if (!tc_eligible(m, n, k)) throw std::string("ERROR (qflex_gb300: tensor cores) --> shape not eligible");
   if (cfg.chunk < 1 || cfg.chunk > 64)
     throw std::string("ERROR (qflex_gb300: tensor cores) --> chunk length must be 1..64");
+  if (a_in_planes && (k < 32 || (k & (k - 1)) != 0 || cfg.chunk > 2))
+    throw std::string("ERROR (qflex_gb300: tensor cores) --> A in planes needs k = 2^j >= 32 and chunk <= 2");
   static std::once_flag attr;
   std::call_once(attr, [] {
     check(cudaFuncSetAttribute(cgemm_fp16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
           "cudaFuncSetAttribute");
   });
   const std::size_t kpad = (k + 15) / 16 * 16;
-  __half* pa = reinterpret_cast<__half*>(workspace);
-  __half* pb = pa + 4 * m * kpad * (std::size_t)batch;
-  int* ea = reinterpret_cast<int*>(pb + 4 * n * kpad * (std::size_t)batch);
-  int* eb = ea + m * (std::size_t)batch;
+  const Fp16Workspace w = fp16_workspace(workspace, m, n, k, batch);
+  __half* pa = static_cast<__half*>(w.a_planes);
+  __half* pb = static_cast<__half*>(w.b_planes);
+  int* ea = a_in_planes ? w.a_block_exps : w.a_exps;
+  int* eb = w.b_exps;
   {
-    dim3 ga((unsigned)std::min<std::uint64_t>((m + 7) / 8, 152 * 16), (unsigned)batch);
-    split_fp16_kernel<<<ga, 256, 0, s>>>(A, pa, ea, m, k, kpad, batch_stride);
+    if (!a_in_planes) {
+      dim3 ga((unsigned)std::min<std::uint64_t>((m + 7) / 8, 152 * 16), (unsigned)batch);
+      split_fp16_kernel<<<ga, 256, 0, s>>>(A, pa, ea, m, k, kpad, batch_stride);
+    }
     dim3 gb((unsigned)std::min<std::uint64_t>((n + 7) / 8, 152 * 16), (unsigned)batch);
     split_fp16_kernel<<<gb, 256, 0, s>>>(Bt, pb, eb, n, k, kpad, bt_stride);
     check(cudaGetLastError(), "split_fp16");
@@ -1131,7 +1159,7 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
   const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
   dim3 grid(persistent_grid(tiles * (std::size_t)batch), 1, 1);
   cgemm_fp16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch, batch_stride, err,
-                                                        cfg.chunk, ea, eb);
+                                                        cfg.chunk, ea, eb, a_in_planes ? (int)(k / 32) : 0);
   check(cudaGetLastError(), "cgemm_fp16x3");
 }
 

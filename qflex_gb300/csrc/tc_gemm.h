@@ -31,14 +31,32 @@ void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size
                          std::size_t k, std::uint64_t ac_stride, std::uint64_t bt_stride, int batch,
                          float* workspace, int* err, const TcConfig& cfg, cudaStream_t s);
 
+// Where the 3xFP16 product keeps its operands in `workspace` (batch entries
+// after each other in every region): A planes, Bt planes, the row exponents
+// of A and of Bt, and the block exponents of an A operand that arrives as
+// planes (one per 32 values of a row).
+struct Fp16Workspace {
+  void* a_planes;
+  void* b_planes;
+  int* a_exps;
+  int* b_exps;
+  int* a_block_exps;
+};
+Fp16Workspace fp16_workspace(float* workspace, std::size_t m, std::size_t n, std::size_t k, int batch);
+
 // The same product with 3xFP16 planes: every row of A and of Bt is scaled by
 // a power of two so that its largest component lies in [2^14, 2^15), split
 // into FP16 hi + lo, multiplied as hi*hi + hi*lo + lo*hi on kind::f16
 // tensor cores (twice the TF32 rate) and unscaled in the epilogue. Always
 // the single-CTA kernel; cfg.variant is ignored.
+// With `a_in_planes` the A planes and block exponents are already in the
+// workspace (written by launch_permute_fp16_planes; k a power of two >= 32,
+// cfg.chunk <= 2 so that a TMEM chunk never spans two exponent blocks) and
+// A is not read.
 void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size_t m, std::size_t n,
                          std::size_t k, std::uint64_t ac_stride, std::uint64_t bt_stride, int batch,
-                         float* workspace, int* err, const TcConfig& cfg, cudaStream_t s);
+                         float* workspace, int* err, const TcConfig& cfg, cudaStream_t s,
+                         bool a_in_planes = false);
 
 // The same product with BF16x3 planes: x = b0 + b1 + b2 in BF16 (no
 // scaling: BF16 has the FP32 exponent range), six products per real

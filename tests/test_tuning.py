@@ -12,11 +12,12 @@ from tests.conftest import rel_err
 def test_options_round_trip_and_validation(built_lib):
     c = Context(-1, TF32X3)
     assert c.get_option("tc_chunk") >= 1
-    for name, value in (("tc_chunk", 4), ("tc_pair", 0), ("graphs", 0), ("max_batch", 3)):
+    for name, value in (("tc_chunk", 4), ("tc_pair", 0), ("graphs", 0), ("max_batch", 3), ("fuse_splits", 0),
+                        ("open_terminals", 0)):
         c.set_option(name, value)
         assert c.get_option(name) == value
     for name, value in (("tc_chunk", 0), ("tc_chunk", 65), ("tc_chunk", 1.5), ("tc_pair", 2),
-                        ("graphs", -1), ("max_batch", -1), ("no_such_option", 1)):
+                        ("graphs", -1), ("max_batch", -1), ("fuse_splits", 2), ("no_such_option", 1)):
         with pytest.raises(QflexGb300Error):
             c.set_option(name, value)
     with pytest.raises(QflexGb300Error):
@@ -77,3 +78,27 @@ def test_autotune_sets_choices(built_lib, tmp_path):
     assert again["cached"] and again["max_batch"] == res["max_batch"]
     out = ctx.evaluate_many(circuit, ordering, grid, initial, finals, 1 << 40)
     assert np.isfinite([abs(a) for _, a in out]).all()
+
+
+@pytest.mark.gpu
+def test_fused_fp16_planes_match_split(built_lib):
+    """3xFP16 with permutations writing the products' A planes directly
+    (per-32-value scales) against the separate split (per-row scales) and
+    the FP64 oracle, on the 6x6 workload and one 7x7 slice."""
+    from oracle import qflex_oracle as qo
+    from qflex_gb300 import FP16X3
+    cases = [rqc.workload("c2")[:4] + (rqc.workload("c2")[4][:3],)]
+    c7 = rqc.random_circuit(7, 7, 32, seed=0)
+    cases.append((c7, rqc.ordering_7x7((0,), (1,)), rqc.grid_text(7, 7), "", rqc.random_bitstrings(49, 2, 5)))
+    for circuit, ordering, grid, initial, finals in cases:
+        fused, split = Context(0, FP16X3), Context(0, FP16X3)
+        split.set_option("fuse_splits", 0)
+        a = [x for _, x in fused.evaluate_many(circuit, ordering, grid, initial, finals, 1 << 40)]
+        b = [x for _, x in split.evaluate_many(circuit, ordering, grid, initial, finals, 1 << 40)]
+        assert fused.stats()["launches"] < split.stats()["launches"]
+        want = []
+        for f in finals:
+            inp = qo.Input(qo.Circuit.loads(circuit), qo.load_ordering(ordering), qo.Grid.loads(grid), initial, f)
+            want.append(qo.evaluate_circuit(inp, np.complex128, float(1 << 40))[0][1])
+        assert rel_err(a, want) < 1e-5 and rel_err(b, want) < 1e-5
+        assert rel_err(a, b) < 1e-5
