@@ -189,15 +189,21 @@ __global__ void __launch_bounds__(256) permute_kernel(const __grid_constant__ Pe
       float mx = fmaxf(fabsf(v.x), fabsf(v.y));
 #pragma unroll
       for (int w = 16; w; w >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, w));
+      // e with mx * 2^e in [2^14, 2^15), from the exponent bits of mx
+      // (mx in [2^(E-127), 2^(E-126)) for a normal mx of biased exponent E).
       int e = 0;
       if (mx > 0.f && isfinite(mx)) {
-        int ex;
-        frexpf(mx, &ex);  // mx in [2^(ex-1), 2^ex)
+        const int E = int(__float_as_uint(mx) >> 23);
+        int ex = E - 126;
+        if (E == 0) frexpf(mx, &ex);  // subnormal
         e = 15 - ex;
       }
       const std::uint64_t k = std::uint64_t(1) << po.k_log2;
       const std::uint64_t row = o >> po.k_log2, kk = o & (k - 1);
-      const float xr = ldexpf(v.x, e), xi = ldexpf(v.y, e);
+      // Scaling by 2^e is exact: a multiply when 2^e is a normal float.
+      const bool direct = e >= -126 && e <= 127;
+      const float sc = __uint_as_float(std::uint32_t(direct ? e + 127 : 127) << 23);
+      const float xr = direct ? v.x * sc : ldexpf(v.x, e), xi = direct ? v.y * sc : ldexpf(v.y, e);
       const __half rh = __float2half_rn(xr), ih = __float2half_rn(xi);
       __half* pl = po.planes + std::uint64_t(blockIdx.y) * 4 * po.rows * k + ((kk / 16) * po.rows + row) * 64 +
                    (kk % 16);
