@@ -139,7 +139,7 @@ struct PlaneOut {
 };
 
 template <bool PLANES>
-__global__ void __launch_bounds__(256) permute_kernel(const __grid_constant__ PermPlan P,
+__global__ void __launch_bounds__(256, 8) permute_kernel(const __grid_constant__ PermPlan P,
                                                       const float2* __restrict__ src,
                                                       float2* __restrict__ dst,
                                                       std::uint64_t batch_stride, PlaneOut po) {
