@@ -9,7 +9,9 @@
 // (hi*hi + hi*lo + lo*hi) and the complex product uses four real products:
 //   C_re = Ar Br - Ai Bi,   C_im = Ar Bi + Ai Br,
 // i.e. 12 TF32 MMAs per k-step. The minus sign is the instruction
-// descriptor's negate-A bit.
+// descriptor's negate-A bit. The 3xFP16 kind (below) instead keeps a
+// negated copy of Bt's imaginary planes so that one N = 256 MMA yields C_re
+// and C_im side by side: 6 MMAs per k-step, each twice as large.
 //
 // Accumulation. The tensor core accumulates in FP32 but rounds toward zero,
 // so a long sum in one TMEM accumulator drifts in proportion to the number
@@ -54,6 +56,10 @@ constexpr int STAGES = 5;
 constexpr int TILE_A = BM * 128;
 constexpr int TILE_B = BN * 128;
 constexpr int STAGE_BYTES = TILE_A + TILE_B;
+// 3xFP16 stage: five blocks of 128 rows x 64 bytes (one k-step of hi and lo
+// in the 64-byte swizzle): A re, A im, B -im, B re, B im.
+constexpr int F16_BLOCK = BM * 64;
+constexpr int F16_STAGE_BYTES = 5 * F16_BLOCK;
 constexpr int EPI_WARPS = 8;
 constexpr int TMEM_COLS = 4 * BN;         // two chunk buffers of (re, im)
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
@@ -224,8 +230,8 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
                                                  const int* __restrict__ exp_b, int a_blocks) {
   constexpr int KSTEP = KIND == KIND_TF32 ? 8 : 16;  // k values per plane row of 32 bytes
   constexpr int TAIL = BM * 64;                       // BF16 third-piece tile of one operand
-  constexpr int NST = KIND == KIND_BF16 ? 3 : STAGES;
-  constexpr int SBYTES = KIND == KIND_BF16 ? 2 * (TILE_A + TAIL) : STAGE_BYTES;
+  constexpr int NST = KIND == KIND_BF16 ? 3 : (KIND == KIND_FP16 ? 4 : STAGES);
+  constexpr int SBYTES = KIND == KIND_BF16 ? 2 * (TILE_A + TAIL) : (KIND == KIND_FP16 ? F16_STAGE_BYTES : STAGE_BYTES);
   static_assert(NST * SBYTES <= STAGES * STAGE_BYTES, "stages fit the shared memory of the launch");
   extern __shared__ __align__(1024) std::uint8_t smem_raw[];
   std::uint8_t* smem = reinterpret_cast<std::uint8_t*>((reinterpret_cast<std::uintptr_t>(smem_raw) + 1023) &
@@ -293,8 +299,17 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
         if (g >= NST && !mbar_wait(&empty[s], ((g / NST) - 1) & 1, abort_flag, err, 1)) break;
         std::uint8_t* st = smem + s * SBYTES;
         mbar_expect_tx(&full[s], SBYTES);
-        tma_load_4d(map_a, &full[s], st, 0, m0, kb, batch);
-        tma_load_4d(map_b, &full[s], st + TILE_A, 0, n0, kb, batch);
+        if constexpr (KIND == KIND_FP16) {
+          // Planes x = 0 (re hi, lo), 32 (im hi, lo) and, for B, 64 (-im).
+          tma_load_4d(map_a, &full[s], st, 0, m0, kb, batch);
+          tma_load_4d(map_a, &full[s], st + F16_BLOCK, 32, m0, kb, batch);
+          tma_load_4d(map_b, &full[s], st + 2 * F16_BLOCK, 64, n0, kb, batch);
+          tma_load_4d(map_b, &full[s], st + 3 * F16_BLOCK, 0, n0, kb, batch);
+          tma_load_4d(map_b, &full[s], st + 4 * F16_BLOCK, 32, n0, kb, batch);
+        } else {
+          tma_load_4d(map_a, &full[s], st, 0, m0, kb, batch);
+          tma_load_4d(map_b, &full[s], st + TILE_A, 0, n0, kb, batch);
+        }
         if constexpr (KIND == KIND_BF16) {
           tma_load_4d(map_a2, &full[s], st + 2 * TILE_A, 0, m0, kb, batch);
           tma_load_4d(map_b2, &full[s], st + 2 * TILE_A + TAIL, 0, n0, kb, batch);
@@ -340,62 +355,82 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
         }
         const std::uint32_t d_re = tmem + buf * 2 * BN, d_im = d_re + BN;
         const std::uint32_t a0 = smem_u32(smem + s * SBYTES);
-        const std::uint32_t b0 = a0 + TILE_A;
-        const std::uint64_t arh = smem_desc_sw128(a0), arl = smem_desc_sw128(a0 + 32),
-                            aih = smem_desc_sw128(a0 + 64), ail = smem_desc_sw128(a0 + 96);
-        const std::uint64_t brh = smem_desc_sw128(b0), brl = smem_desc_sw128(b0 + 32),
-                            bih = smem_desc_sw128(b0 + 64), bil = smem_desc_sw128(b0 + 96);
         const std::uint32_t acc = first ? 0u : 1u;
-        if constexpr (KIND == KIND_BF16) {
-          // Pieces 0 and 1 sit in the 128-byte rows (re0 re1 im0 im1, named
-          // *h and *l above), piece 2 in the 64-byte rows (re2 im2). Per real
-          // product x*y the terms x2y0, x1y1, x0y2 (~2^-16), x1y0, x0y1
-          // (~2^-8) and x0y0, smallest first.
-          const std::uint32_t at = a0 + 2 * TILE_A, bt = at + TAIL;
-          const std::uint64_t ar2 = smem_desc_sw64(at), ai2 = smem_desc_sw64(at + 32);
-          const std::uint64_t br2 = smem_desc_sw64(bt), bi2 = smem_desc_sw64(bt + 32);
-          // C_re = Ar Br - Ai Bi
-          umma<KIND>(d_re, ar2, brh, idp, acc);
-          umma<KIND>(d_re, arl, brl, idp, 1);
-          umma<KIND>(d_re, arh, br2, idp, 1);
-          umma<KIND>(d_re, ai2, bih, idn, 1);
-          umma<KIND>(d_re, ail, bil, idn, 1);
-          umma<KIND>(d_re, aih, bi2, idn, 1);
-          umma<KIND>(d_re, arl, brh, idp, 1);
-          umma<KIND>(d_re, arh, brl, idp, 1);
-          umma<KIND>(d_re, ail, bih, idn, 1);
-          umma<KIND>(d_re, aih, bil, idn, 1);
-          umma<KIND>(d_re, arh, brh, idp, 1);
-          umma<KIND>(d_re, aih, bih, idn, 1);
-          // C_im = Ar Bi + Ai Br
-          umma<KIND>(d_im, ar2, bih, idp, acc);
-          umma<KIND>(d_im, arl, bil, idp, 1);
-          umma<KIND>(d_im, arh, bi2, idp, 1);
-          umma<KIND>(d_im, ai2, brh, idp, 1);
-          umma<KIND>(d_im, ail, brl, idp, 1);
-          umma<KIND>(d_im, aih, br2, idp, 1);
-          umma<KIND>(d_im, arl, bih, idp, 1);
-          umma<KIND>(d_im, arh, bil, idp, 1);
-          umma<KIND>(d_im, ail, brh, idp, 1);
-          umma<KIND>(d_im, aih, brl, idp, 1);
-          umma<KIND>(d_im, arh, bih, idp, 1);
-          umma<KIND>(d_im, aih, brh, idp, 1);
+        if constexpr (KIND == KIND_FP16) {
+          // One M = 128, N = 256 product gives C_re (columns 0..127) and
+          // C_im (128..255) together: Ar against the B rows (Br; Bi) and Ai
+          // against (-Bi; Br), both read from the stage's B blocks
+          // (-Bi, Br, Bi). Six MMAs per k-step, small terms first.
+          const std::uint32_t idw = idesc_f16(BM, 2 * BN, false);
+          const std::uint32_t ar = a0, ai = a0 + F16_BLOCK, bn = a0 + 2 * F16_BLOCK, br = a0 + 3 * F16_BLOCK;
+          const std::uint64_t arh = smem_desc_sw64(ar), arl = smem_desc_sw64(ar + 32);
+          const std::uint64_t aih = smem_desc_sw64(ai), ail = smem_desc_sw64(ai + 32);
+          const std::uint64_t b1h = smem_desc_sw64(br), b1l = smem_desc_sw64(br + 32);
+          const std::uint64_t b2h = smem_desc_sw64(bn), b2l = smem_desc_sw64(bn + 32);
+          umma<KIND>(d_re, arh, b1l, idw, acc);
+          umma<KIND>(d_re, arl, b1h, idw, 1);
+          umma<KIND>(d_re, aih, b2l, idw, 1);
+          umma<KIND>(d_re, ail, b2h, idw, 1);
+          umma<KIND>(d_re, arh, b1h, idw, 1);
+          umma<KIND>(d_re, aih, b2h, idw, 1);
+          (void)d_im;
         } else {
-          // The small hi*lo terms go first and the two large hi*hi terms
-          // last, so only those two additions round against a large
-          // accumulator.
-          umma<KIND>(d_re, arh, brl, idp, acc);
-          umma<KIND>(d_re, arl, brh, idp, 1);
-          umma<KIND>(d_re, aih, bil, idn, 1);
-          umma<KIND>(d_re, ail, bih, idn, 1);
-          umma<KIND>(d_re, arh, brh, idp, 1);
-          umma<KIND>(d_re, aih, bih, idn, 1);
-          umma<KIND>(d_im, arh, bil, idp, acc);
-          umma<KIND>(d_im, arl, bih, idp, 1);
-          umma<KIND>(d_im, aih, brl, idp, 1);
-          umma<KIND>(d_im, ail, brh, idp, 1);
-          umma<KIND>(d_im, arh, bih, idp, 1);
-          umma<KIND>(d_im, aih, brh, idp, 1);
+          const std::uint32_t b0 = a0 + TILE_A;
+          const std::uint64_t arh = smem_desc_sw128(a0), arl = smem_desc_sw128(a0 + 32),
+                              aih = smem_desc_sw128(a0 + 64), ail = smem_desc_sw128(a0 + 96);
+          const std::uint64_t brh = smem_desc_sw128(b0), brl = smem_desc_sw128(b0 + 32),
+                              bih = smem_desc_sw128(b0 + 64), bil = smem_desc_sw128(b0 + 96);
+          if constexpr (KIND == KIND_BF16) {
+            // Pieces 0 and 1 sit in the 128-byte rows (re0 re1 im0 im1, named
+            // *h and *l above), piece 2 in the 64-byte rows (re2 im2). Per real
+            // product x*y the terms x2y0, x1y1, x0y2 (~2^-16), x1y0, x0y1
+            // (~2^-8) and x0y0, smallest first.
+            const std::uint32_t at = a0 + 2 * TILE_A, bt = at + TAIL;
+            const std::uint64_t ar2 = smem_desc_sw64(at), ai2 = smem_desc_sw64(at + 32);
+            const std::uint64_t br2 = smem_desc_sw64(bt), bi2 = smem_desc_sw64(bt + 32);
+            // C_re = Ar Br - Ai Bi
+            umma<KIND>(d_re, ar2, brh, idp, acc);
+            umma<KIND>(d_re, arl, brl, idp, 1);
+            umma<KIND>(d_re, arh, br2, idp, 1);
+            umma<KIND>(d_re, ai2, bih, idn, 1);
+            umma<KIND>(d_re, ail, bil, idn, 1);
+            umma<KIND>(d_re, aih, bi2, idn, 1);
+            umma<KIND>(d_re, arl, brh, idp, 1);
+            umma<KIND>(d_re, arh, brl, idp, 1);
+            umma<KIND>(d_re, ail, bih, idn, 1);
+            umma<KIND>(d_re, aih, bil, idn, 1);
+            umma<KIND>(d_re, arh, brh, idp, 1);
+            umma<KIND>(d_re, aih, bih, idn, 1);
+            // C_im = Ar Bi + Ai Br
+            umma<KIND>(d_im, ar2, bih, idp, acc);
+            umma<KIND>(d_im, arl, bil, idp, 1);
+            umma<KIND>(d_im, arh, bi2, idp, 1);
+            umma<KIND>(d_im, ai2, brh, idp, 1);
+            umma<KIND>(d_im, ail, brl, idp, 1);
+            umma<KIND>(d_im, aih, br2, idp, 1);
+            umma<KIND>(d_im, arl, bih, idp, 1);
+            umma<KIND>(d_im, arh, bil, idp, 1);
+            umma<KIND>(d_im, ail, brh, idp, 1);
+            umma<KIND>(d_im, aih, brl, idp, 1);
+            umma<KIND>(d_im, arh, bih, idp, 1);
+            umma<KIND>(d_im, aih, brh, idp, 1);
+          } else {
+            // The small hi*lo terms go first and the two large hi*hi terms
+            // last, so only those two additions round against a large
+            // accumulator.
+            umma<KIND>(d_re, arh, brl, idp, acc);
+            umma<KIND>(d_re, arl, brh, idp, 1);
+            umma<KIND>(d_re, aih, bil, idn, 1);
+            umma<KIND>(d_re, ail, bih, idn, 1);
+            umma<KIND>(d_re, arh, brh, idp, 1);
+            umma<KIND>(d_re, aih, bih, idn, 1);
+            umma<KIND>(d_im, arh, bil, idp, acc);
+            umma<KIND>(d_im, arl, bih, idp, 1);
+            umma<KIND>(d_im, aih, brl, idp, 1);
+            umma<KIND>(d_im, ail, brh, idp, 1);
+            umma<KIND>(d_im, arh, bih, idp, 1);
+            umma<KIND>(d_im, aih, brh, idp, 1);
+          }
         }
         umma_commit(&empty[s]);
         if (kb % CHUNK == CHUNK - 1 || kb == kblocks - 1) {
@@ -855,14 +890,16 @@ __global__ void __launch_bounds__(256) split_tf32_kernel(const float2* __restric
 // 65504), then hi = fp16(x 2^e) and lo = fp16(x 2^e - hi) for re and im,
 // both round-to-nearest, so x 2^e = hi + lo to ~22 significant bits.
 // Output per batch entry: planes [k / 16][row][plane][16] fp16 (re_hi,
-// re_lo, im_hi, im_lo; one 128-byte row per k-step, k zero-padded to a
-// multiple of 16) and the exponents [row] (int).
+// re_lo, im_hi, im_lo, and with nplanes = 6 also -im_hi, -im_lo; one 128- or
+// 192-byte row per k-step, k zero-padded to a multiple of 16) and the
+// exponents [row] (int).
 __global__ void __launch_bounds__(256) split_fp16_kernel(const float2* __restrict__ src, __half* __restrict__ planes,
                                                          int* __restrict__ exps, std::uint64_t rows, std::uint64_t k,
-                                                         std::uint64_t kpad, std::uint64_t src_batch_stride) {
+                                                         std::uint64_t kpad, std::uint64_t src_batch_stride,
+                                                         int nplanes) {
   const std::uint64_t b = blockIdx.y;
   const float2* sb = src + b * src_batch_stride;
-  __half* pb = planes + b * 4 * rows * kpad;
+  __half* pb = planes + b * nplanes * rows * kpad;
   int* eb = exps + b * rows;
   const int lane = threadIdx.x % 32;
   const std::uint64_t warps = std::uint64_t(gridDim.x) * (blockDim.x / 32);
@@ -891,11 +928,16 @@ __global__ void __launch_bounds__(256) split_fp16_kernel(const float2* __restric
       const float r0 = ldexpf(v0.x, e), i0 = ldexpf(v0.y, e), r1 = ldexpf(v1.x, e), i1 = ldexpf(v1.y, e);
       const __half2 rh = __floats2half2_rn(r0, r1), ih = __floats2half2_rn(i0, i1);
       const float2 rhf = __half22float2(rh), ihf = __half22float2(ih);
-      __half* o = pb + ((kk / 16) * rows + row) * 64 + (kk % 16);
+      __half* o = pb + ((kk / 16) * rows + row) * (16 * nplanes) + (kk % 16);
+      const __half2 il = __floats2half2_rn(i0 - ihf.x, i1 - ihf.y);
       *reinterpret_cast<__half2*>(o) = rh;
       *reinterpret_cast<__half2*>(o + 16) = __floats2half2_rn(r0 - rhf.x, r1 - rhf.y);
       *reinterpret_cast<__half2*>(o + 32) = ih;
-      *reinterpret_cast<__half2*>(o + 48) = __floats2half2_rn(i0 - ihf.x, i1 - ihf.y);
+      *reinterpret_cast<__half2*>(o + 48) = il;
+      if (nplanes == 6) {
+        *reinterpret_cast<__half2*>(o + 64) = __hneg2(ih);
+        *reinterpret_cast<__half2*>(o + 80) = __hneg2(il);
+      }
     }
   }
 }
@@ -977,18 +1019,21 @@ CUtensorMap plane_map(const float* base, std::uint64_t rows, std::uint64_t kpad,
   return map;
 }
 
-// 4-D map over FP16 planes laid out [batch][kpad / 16][rows][64] (fp16),
-// box {64, box_rows, 1, 1} (one 128-byte row per tile row), 128-byte swizzle.
-CUtensorMap plane_map_f16(const __half* base, std::uint64_t rows, std::uint64_t kpad, int batch, int box_rows) {
+// 4-D map over FP16 planes laid out [batch][kpad / 16][rows][row_halves]
+// (64: re hi, lo, im hi, lo; 96: also -im hi, lo), box {32, box_rows, 1, 1}:
+// the hi and lo planes of one part as 64-byte rows, 64-byte swizzle; the
+// part is chosen by the box's x coordinate (0, 32, 64).
+CUtensorMap plane_map_f16(const __half* base, std::uint64_t rows, std::uint64_t kpad, int batch, int box_rows,
+                          int row_halves) {
   CUtensorMap map;
   std::memset(&map, 0, sizeof(map));
-  const std::uint64_t kb = kpad / 16;
-  const cuuint64_t dims[4] = {64, rows, kb, (cuuint64_t)batch};
-  const cuuint64_t strides[3] = {128, rows * 128, kb * rows * 128};
-  const cuuint32_t box[4] = {64, (cuuint32_t)box_rows, 1, 1};
+  const std::uint64_t kb = kpad / 16, rb = std::uint64_t(row_halves) * 2;
+  const cuuint64_t dims[4] = {(cuuint64_t)row_halves, rows, kb, (cuuint64_t)batch};
+  const cuuint64_t strides[3] = {rb, rows * rb, kb * rows * rb};
+  const cuuint32_t box[4] = {32, (cuuint32_t)box_rows, 1, 1};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 4, const_cast<__half*>(base), dims, strides, box,
-                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS)
     throw std::string("ERROR (qflex_gb300: tensor cores) --> cuTensorMapEncodeTiled failed: ") +
@@ -1030,10 +1075,10 @@ bool tc_eligible(std::size_t m, std::size_t n, std::size_t k) {
 
 std::size_t tc_workspace_elems(std::size_t m, std::size_t n, std::size_t k) {
   // The largest of the 3xTF32 planes (4 fp32 per element), the 3xFP16
-  // planes (4 fp16 per element) plus their row exponents and the BF16x3
+  // planes (4 fp16 per element of A, 6 of Bt) plus their exponents and the BF16x3
   // planes (6 bf16 per element, fewer than the 3xTF32 ones).
   const std::size_t tf32 = 4 * (m + n) * ((k + 7) / 8 * 8);
-  const std::size_t fp16 = 2 * (m + n) * ((k + 15) / 16 * 16) + (m + n) + m * ((k + 31) / 32) + 64;
+  const std::size_t fp16 = (2 * m + 3 * n) * ((k + 15) / 16 * 16) + (m + n) + m * ((k + 31) / 32) + 64;
   return tf32 > fp16 ? tf32 : fp16;
 }
 
@@ -1120,7 +1165,7 @@ Fp16Workspace fp16_workspace(float* workspace, std::size_t m, std::size_t n, std
   __half* pb = pa + 4 * m * kpad * nb;
   w.a_planes = pa;
   w.b_planes = pb;
-  w.a_exps = reinterpret_cast<int*>(pb + 4 * n * kpad * nb);
+  w.a_exps = reinterpret_cast<int*>(pb + 6 * n * kpad * nb);
   w.b_exps = w.a_exps + m * nb;
   w.a_block_exps = w.b_exps + n * nb;
   return w;
@@ -1148,14 +1193,14 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
   {
     if (!a_in_planes) {
       dim3 ga((unsigned)std::min<std::uint64_t>((m + 7) / 8, 152 * 16), (unsigned)batch);
-      split_fp16_kernel<<<ga, 256, 0, s>>>(A, pa, ea, m, k, kpad, batch_stride);
+      split_fp16_kernel<<<ga, 256, 0, s>>>(A, pa, ea, m, k, kpad, batch_stride, 4);
     }
     dim3 gb((unsigned)std::min<std::uint64_t>((n + 7) / 8, 152 * 16), (unsigned)batch);
-    split_fp16_kernel<<<gb, 256, 0, s>>>(Bt, pb, eb, n, k, kpad, bt_stride);
+    split_fp16_kernel<<<gb, 256, 0, s>>>(Bt, pb, eb, n, k, kpad, bt_stride, 6);
     check(cudaGetLastError(), "split_fp16");
   }
-  const CUtensorMap ma = plane_map_f16(pa, m, kpad, batch, BM);
-  const CUtensorMap mb = plane_map_f16(pb, n, kpad, batch, BN);
+  const CUtensorMap ma = plane_map_f16(pa, m, kpad, batch, BM, 64);
+  const CUtensorMap mb = plane_map_f16(pb, n, kpad, batch, BN, 96);
   const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
   dim3 grid(persistent_grid(tiles * (std::size_t)batch), 1, 1);
   cgemm_fp16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch, batch_stride, err,
