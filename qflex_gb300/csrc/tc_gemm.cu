@@ -117,6 +117,26 @@ __device__ __forceinline__ void tma_load_4d(const CUtensorMap* map, std::uint64_
       : "memory");
 }
 
+// Bulk tensor store of a shared-memory box to global memory (C tiles), its
+// commit group, and the waits for the box's shared-memory reads / for the
+// global writes to finish.
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, const void* src, int c0, int c1, int c2) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
+                   reinterpret_cast<std::uint64_t>(map)),
+               "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(src))
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// v * 2^e, exact unless the result leaves the normal range (then rounded
+// like ldexpf): a multiply by the power of two when 2^e is a normal float.
+__device__ __forceinline__ float scale2(float v, int e) {
+  return (e >= -126 && e <= 127) ? v * __uint_as_float(std::uint32_t(e + 127) << 23) : ldexpf(v, e);
+}
+
 // Shared-memory matrix descriptor: K-major operand inside rows of 128 bytes
 // in the 128-byte swizzle (the start address may sit 32, 64 or 96 bytes into
 // the row, as for a K offset), 8-row groups 1024 bytes apart.
@@ -224,6 +244,7 @@ __device__ __forceinline__ void mbar_arrive(std::uint64_t* bar) {
 template <int KIND>
 __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const CUtensorMap* map_b,
                                                  const CUtensorMap* map_a2, const CUtensorMap* map_b2,
+                                                 const CUtensorMap* map_c, bool tma_c,
                                                  float2* __restrict__ C, int m, int n, int k, int batches,
                                                  std::uint64_t c_batch_stride, int* __restrict__ err, int CHUNK,
                                                  const int* __restrict__ exp_a,
@@ -457,20 +478,22 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
       float tre[BN / 2], tim[BN / 2];
 #pragma unroll
       for (int j = 0; j < BN / 2; ++j) tre[j] = tim[j] = 0.f;
+      // A's block exponent of a chunk is fetched one chunk ahead, so its
+      // load latency stays out of the drain.
+      const bool blocked = KIND == KIND_FP16 && a_blocks > 0 && m0 + row < m;
+      const int* eblk = blocked ? exp_a + (std::uint64_t(batch) * m + m0 + row) * a_blocks : nullptr;
+      int e_next = blocked ? eblk[0] : 0;
       for (int cc = 0; cc < chunks; ++cc, ++c) {
         const int buf = c & 1;
+        const int e_blk = e_next;
+        if (blocked && cc + 1 < chunks) e_next = eblk[((cc + 1) * CHUNK * KSTEP) / 32];
         if (!mbar_wait(&acc_full[buf], (c >> 1) & 1, abort_flag, err, 3)) {
           ok = false;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
         // Scale of this chunk: 1, or 2^-e of A's block for this row.
-        float sa = 1.f;
-        if (KIND == KIND_FP16 && a_blocks > 0) {
-          const int blk = (cc * CHUNK * KSTEP) / 32;
-          const int e = m0 + row < m ? exp_a[(std::uint64_t(batch) * m + m0 + row) * a_blocks + blk] : 0;
-          sa = ldexpf(1.f, -e);
-        }
+        const float sa = scale2(1.f, -e_blk);
         const std::uint32_t base = tmem + (std::uint32_t(q * 32) << 16) + buf * 2 * BN + half * (BN / 2);
 #pragma unroll
         for (int j0 = 0; j0 < BN / 2; j0 += 32) {
@@ -492,36 +515,77 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
       }
       if (!ok) break;
       // The MMA issuer already works on the next tile. The warp's 32 x 64
-      // block leaves through its staging area as whole 32-column row pieces:
-      // element (r, j) of a 32 x 32 piece sits at r * 32 + (j ^ r).
+      // block leaves in two 32 x 32 pieces through its staging area.
       const int ncols = n - n0 - half * (BN / 2);
-      int ea = 0;
-      const int* eb = nullptr;
+      // 3xFP16 scale exponents: the row's (unless A's blocks were applied
+      // per chunk) and, per piece, that of column j0 + lane.
+      int ea = 0, eb0 = 0, eb1 = 0;
       if (KIND == KIND_FP16) {
         ea = (a_blocks == 0 && m0 + row < m) ? exp_a[std::uint64_t(batch) * m + m0 + row] : 0;
-        eb = exp_b + std::uint64_t(batch) * n + n0 + half * (BN / 2);
+        const int* eb = exp_b + std::uint64_t(batch) * n + n0 + half * (BN / 2);
+        eb0 = lane < ncols ? eb[lane] : 0;
+        eb1 = 32 + lane < ncols ? eb[32 + lane] : 0;
       }
       float2* cb = C + std::uint64_t(batch) * c_batch_stride;
 #pragma unroll
       for (int j0 = 0; j0 < BN / 2; j0 += 32) {
+        const int ebl = j0 ? eb1 : eb0;
+        if (tma_c) {
+          // Two boxes of 32 rows x 16 complex in the 128-byte swizzle (16-byte
+          // unit u of row r at r * 128 + ((u ^ r % 8) * 16)), stored by TMA;
+          // the staging area is rewritten once the previous boxes were read.
+          if (lane == 0) bulk_wait_read();
+          __syncwarp();
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          float2 v = make_float2(tre[j0 + j], tim[j0 + j]);
-          if (KIND == KIND_FP16) {
-            const int e = j0 + j < ncols ? -(ea + eb[j0 + j]) : 0;
-            v = make_float2(ldexpf(v.x, e), ldexpf(v.y, e));
+          for (int j = 0; j < 32; j += 2) {
+            float2 v0 = make_float2(tre[j0 + j], tim[j0 + j]);
+            float2 v1 = make_float2(tre[j0 + j + 1], tim[j0 + j + 1]);
+            if (KIND == KIND_FP16) {
+              const int e0 = -(ea + __shfl_sync(0xffffffffu, ebl, j));
+              const int e1 = -(ea + __shfl_sync(0xffffffffu, ebl, j + 1));
+              v0 = make_float2(scale2(v0.x, e0), scale2(v0.y, e0));
+              v1 = make_float2(scale2(v1.x, e1), scale2(v1.y, e1));
+            }
+            const int u = (j % 16) / 2;
+            float4* dst = reinterpret_cast<float4*>(reinterpret_cast<std::uint8_t*>(stg) + (j / 16) * 4096 +
+                                                    lane * 128 + ((u ^ (lane & 7)) << 4));
+            *dst = make_float4(v0.x, v0.y, v1.x, v1.y);
           }
-          stg[lane * 32 + (j ^ lane)] = v;
+          fence_proxy_async();
+          __syncwarp();
+          if (lane == 0) {
+            const int x = 2 * (n0 + half * (BN / 2) + j0), y = m0 + q * 32;
+            if (y < m) {
+              if (x < 2 * n) tma_store_3d(map_c, stg, x, y, batch);
+              if (x + 32 < 2 * n) tma_store_3d(map_c, reinterpret_cast<std::uint8_t*>(stg) + 4096, x + 32, y, batch);
+            }
+            bulk_commit();
+          }
+        } else {
+          // Element (r, j) of the piece sits at r * 32 + (j ^ r); the warp
+          // stores whole 32-column row pieces.
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            float2 v = make_float2(tre[j0 + j], tim[j0 + j]);
+            if (KIND == KIND_FP16) {
+              const int e = -(ea + __shfl_sync(0xffffffffu, ebl, j));
+              v = make_float2(scale2(v.x, e), scale2(v.y, e));
+            }
+            stg[lane * 32 + (j ^ lane)] = v;
+          }
+          __syncwarp();
+          for (int r = 0; r < 32; ++r) {
+            const int gr = m0 + q * 32 + r;
+            if (gr < m && j0 + lane < ncols)
+              cb[std::uint64_t(gr) * n + n0 + half * (BN / 2) + j0 + lane] = stg[r * 32 + (lane ^ r)];
+          }
+          __syncwarp();
         }
-        __syncwarp();
-        for (int r = 0; r < 32; ++r) {
-          const int gr = m0 + q * 32 + r;
-          if (gr < m && j0 + lane < ncols)
-            cb[std::uint64_t(gr) * n + n0 + half * (BN / 2) + j0 + lane] = stg[r * 32 + (lane ^ r)];
-        }
-        __syncwarp();
       }
     }
+    // Every bulk store has written global memory before the CTA ends.
+    if (tma_c && lane == 0) bulk_wait_all();
+    __syncwarp();
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -538,27 +602,27 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
 
 __global__ void __launch_bounds__(THREADS, 1)
     cgemm_tf32x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
-                        float2* __restrict__ C, int m, int n, int k, int batches, std::uint64_t c_batch_stride,
-                        int* __restrict__ err, int CHUNK) {
-  cgemm_split_body<KIND_TF32>(&map_a, &map_b, nullptr, nullptr, C, m, n, k, batches, c_batch_stride, err, CHUNK,
+                        const __grid_constant__ CUtensorMap map_c, int tma_c, float2* __restrict__ C, int m, int n,
+                        int k, int batches, std::uint64_t c_batch_stride, int* __restrict__ err, int CHUNK) {
+  cgemm_split_body<KIND_TF32>(&map_a, &map_b, nullptr, nullptr, &map_c, tma_c != 0, C, m, n, k, batches, c_batch_stride, err, CHUNK,
                               nullptr, nullptr, 0);
 }
 
 __global__ void __launch_bounds__(THREADS, 1)
     cgemm_fp16x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
-                        float2* __restrict__ C, int m, int n, int k, int batches, std::uint64_t c_batch_stride,
-                        int* __restrict__ err, int CHUNK, const int* __restrict__ exp_a,
-                        const int* __restrict__ exp_b, int a_blocks) {
-  cgemm_split_body<KIND_FP16>(&map_a, &map_b, nullptr, nullptr, C, m, n, k, batches, c_batch_stride, err, CHUNK,
+                        const __grid_constant__ CUtensorMap map_c, int tma_c, float2* __restrict__ C, int m, int n,
+                        int k, int batches, std::uint64_t c_batch_stride, int* __restrict__ err, int CHUNK,
+                        const int* __restrict__ exp_a, const int* __restrict__ exp_b, int a_blocks) {
+  cgemm_split_body<KIND_FP16>(&map_a, &map_b, nullptr, nullptr, &map_c, tma_c != 0, C, m, n, k, batches, c_batch_stride, err, CHUNK,
                               exp_a, exp_b, a_blocks);
 }
 
 __global__ void __launch_bounds__(THREADS, 1)
     cgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                         const __grid_constant__ CUtensorMap map_a2, const __grid_constant__ CUtensorMap map_b2,
-                        float2* __restrict__ C, int m, int n, int k, int batches, std::uint64_t c_batch_stride,
-                        int* __restrict__ err, int CHUNK) {
-  cgemm_split_body<KIND_BF16>(&map_a, &map_b, &map_a2, &map_b2, C, m, n, k, batches, c_batch_stride, err, CHUNK,
+                        const __grid_constant__ CUtensorMap map_c, int tma_c, float2* __restrict__ C, int m, int n,
+                        int k, int batches, std::uint64_t c_batch_stride, int* __restrict__ err, int CHUNK) {
+  cgemm_split_body<KIND_BF16>(&map_a, &map_b, &map_a2, &map_b2, &map_c, tma_c != 0, C, m, n, k, batches, c_batch_stride, err, CHUNK,
                               nullptr, nullptr, 0);
 }
 
@@ -1063,6 +1127,27 @@ CUtensorMap plane_map_bf16(const __nv_bfloat16* base, std::uint64_t rows, std::u
   return map;
 }
 
+// 3-D map over C as floats [batch][m][2n] for the epilogue's bulk stores,
+// box {32, 32, 1} (32 rows x 16 complex) in the 128-byte swizzle. False (and
+// the epilogue stores with plain instructions) when C is not 16-byte
+// aligned, n or the batch stride is odd, or QFLEX_TC_TMA_STORE=0.
+bool output_map(float2* C, std::size_t m, std::size_t n, std::uint64_t batch_stride, int batch, CUtensorMap* map) {
+  static const bool enabled = [] {
+    const char* e = std::getenv("QFLEX_TC_TMA_STORE");
+    return !(e && std::atoi(e) == 0);
+  }();
+  std::memset(map, 0, sizeof(*map));
+  if (!enabled || (reinterpret_cast<std::uintptr_t>(C) & 15) || (n & 1) || (batch > 1 && (batch_stride & 1)))
+    return false;
+  const cuuint64_t dims[3] = {2 * n, m, (cuuint64_t)batch};
+  const cuuint64_t strides[2] = {n * 8, (batch > 1 ? batch_stride : m * n) * 8};
+  const cuuint32_t box[3] = {32, 32, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, C, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 void check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw std::string("ERROR (qflex_gb300: CUDA ") + what + ") --> " + cudaGetErrorString(e);
 }
@@ -1153,8 +1238,10 @@ void launch_cgemm_tf32x3(const float2* A, const float2* Bt, float2* C, std::size
   const CUtensorMap mb = plane_map(pb, n, kpad, batch, BN);
   const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
   dim3 grid(persistent_grid(tiles * (std::size_t)batch), 1, 1);
-  cgemm_tf32x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch, batch_stride, err,
-                                                        chunk);
+  CUtensorMap mc;
+  const int tma_c = output_map(C, m, n, batch_stride, batch, &mc) ? 1 : 0;
+  cgemm_tf32x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, mc, tma_c, C, (int)m, (int)n, (int)k, batch,
+                                                        batch_stride, err, chunk);
   check(cudaGetLastError(), "cgemm_tf32x3");
 }
 
@@ -1203,8 +1290,11 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
   const CUtensorMap mb = plane_map_f16(pb, n, kpad, batch, BN, 96);
   const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
   dim3 grid(persistent_grid(tiles * (std::size_t)batch), 1, 1);
-  cgemm_fp16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, C, (int)m, (int)n, (int)k, batch, batch_stride, err,
-                                                        cfg.chunk, ea, eb, a_in_planes ? (int)(k / 32) : 0);
+  CUtensorMap mc;
+  const int tma_c = output_map(C, m, n, batch_stride, batch, &mc) ? 1 : 0;
+  cgemm_fp16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, mc, tma_c, C, (int)m, (int)n, (int)k, batch,
+                                                        batch_stride, err, cfg.chunk, ea, eb,
+                                                        a_in_planes ? (int)(k / 32) : 0);
   check(cudaGetLastError(), "cgemm_fp16x3");
 }
 
@@ -1238,8 +1328,10 @@ void launch_cgemm_bf16x3(const float2* A, const float2* Bt, float2* C, std::size
   const CUtensorMap mb2 = plane_map_bf16(bt, n, kpad, batch, BN, 32);
   const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
   dim3 grid(persistent_grid(tiles * (std::size_t)batch), 1, 1);
-  cgemm_bf16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, ma2, mb2, C, (int)m, (int)n, (int)k, batch, batch_stride,
-                                                        err, cfg.chunk);
+  CUtensorMap mc;
+  const int tma_c = output_map(C, m, n, batch_stride, batch, &mc) ? 1 : 0;
+  cgemm_bf16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, ma2, mb2, mc, tma_c, C, (int)m, (int)n, (int)k, batch,
+                                                        batch_stride, err, cfg.chunk);
   check(cudaGetLastError(), "cgemm_bf16x3");
 }
 

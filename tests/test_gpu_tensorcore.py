@@ -20,10 +20,13 @@ def tc_ctx(built_lib, request):
     return Context(0, request.param)
 
 
-# Ragged m and n leave whole tiles partly outside the matrix.
+# Ragged m and n leave whole tiles partly outside the matrix; an odd n
+# (97, 131) takes the epilogue's plain stores instead of the bulk tensor
+# stores.
 @pytest.mark.parametrize("m,n,k", [(128, 128, 16), (64, 64, 16), (256, 512, 128), (1024, 256, 256),
                                    (300, 128, 64), (128, 1024, 40), (4096, 256, 256), (256, 64, 16),
-                                   (512, 96, 24), (768, 200, 100), (2048, 2048, 2048)])
+                                   (512, 96, 24), (768, 200, 100), (2048, 2048, 2048), (256, 97, 64),
+                                   (200, 131, 48)])
 def test_tf32x3_multiply(tc_ctx, m, n, k):
     import torch
     g = np.random.default_rng(m + 7 * n + 13 * k)
@@ -152,3 +155,27 @@ def test_tf32x3_pair_kernel(built_lib, m, n, k):
     want = A.astype(np.complex128) @ B.astype(np.complex128)
     assert np.isfinite(got).all()
     assert np.max(np.abs(got - want)) / np.mean(np.abs(want)) < 2e-5
+
+
+@pytest.mark.parametrize("extra", [0, 1], ids=["even_stride", "odd_stride"])
+def test_tensorcore_multiply_batched(tc_ctx, extra):
+    """Batched products with the batch entries `stride` complex apart; an odd
+    stride takes the plain-store epilogue, an even one the bulk stores."""
+    import torch
+    m, n, k, batch = 192, 96, 48, 3
+    stride = m * k + k * n + m * n + extra
+    g = np.random.default_rng(11 + extra)
+    buf = (g.standard_normal((batch, stride)) + 1j * g.standard_normal((batch, stride))).astype(np.complex64)
+    d = torch.from_numpy(buf).cuda()
+    base = d.data_ptr()
+    torch.cuda.synchronize()
+    tc_ctx.multiply(base, base + 8 * m * k, base + 8 * (m * k + k * n), m, n, k, batch, stride)
+    tc_ctx.synchronize()
+    out = d.cpu().numpy()
+    for b in range(batch):
+        A = buf[b, :m * k].reshape(m, k).astype(np.complex128)
+        B = buf[b, m * k:m * k + k * n].reshape(k, n).astype(np.complex128)
+        C = out[b, m * k + k * n:m * k + k * n + m * n].reshape(m, n)
+        want = A @ B
+        assert np.max(np.abs(C - want)) / np.mean(np.abs(want)) < 2e-5, b
+        assert np.array_equal(out[b, m * k + k * n + m * n:], buf[b, m * k + k * n + m * n:])
