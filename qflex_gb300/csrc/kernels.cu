@@ -186,16 +186,19 @@ __global__ void __launch_bounds__(256, 8) permute_kernel(const __grid_constant__
       }
       // The warp's 32 values are outputs o - lane .. o - lane + 31: one
       // 32-aligned run of a row (the tile holds the 5 lowest output digits).
-      float mx = fmaxf(fabsf(v.x), fabsf(v.y));
-#pragma unroll
-      for (int w = 16; w; w >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, w));
-      // e with mx * 2^e in [2^14, 2^15), from the exponent bits of mx
-      // (mx in [2^(E-127), 2^(E-126)) for a normal mx of biased exponent E).
+      // Its largest |re| or |im|: bit patterns of non-negative floats order
+      // like their values, so one integer warp reduction finds it.
+      const std::uint32_t mb = __reduce_max_sync(
+          0xffffffffu, max(__float_as_uint(fabsf(v.x)), __float_as_uint(fabsf(v.y))));
+      // e with max * 2^e in [2^14, 2^15): a normal max of biased exponent E
+      // lies in [2^(E-127), 2^(E-126)); infinities and NaN keep e = 0.
+      const int E = int(mb >> 23);
       int e = 0;
-      if (mx > 0.f && isfinite(mx)) {
-        const int E = int(__float_as_uint(mx) >> 23);
-        int ex = E - 126;
-        if (E == 0) frexpf(mx, &ex);  // subnormal
+      if (E > 0 && E < 255) {
+        e = 141 - E;
+      } else if (E == 0 && mb != 0) {
+        int ex;
+        frexpf(__uint_as_float(mb), &ex);  // subnormal
         e = 15 - ex;
       }
       const std::uint64_t k = std::uint64_t(1) << po.k_log2;
@@ -204,13 +207,15 @@ __global__ void __launch_bounds__(256, 8) permute_kernel(const __grid_constant__
       const bool direct = e >= -126 && e <= 127;
       const float sc = __uint_as_float(std::uint32_t(direct ? e + 127 : 127) << 23);
       const float xr = direct ? v.x * sc : ldexpf(v.x, e), xi = direct ? v.y * sc : ldexpf(v.y, e);
-      const __half rh = __float2half_rn(xr), ih = __float2half_rn(xi);
+      const __half2 hi = __floats2half2_rn(xr, xi);  // (re_hi, im_hi)
+      const float2 hf = __half22float2(hi);
+      const __half2 lo = __floats2half2_rn(xr - hf.x, xi - hf.y);
       __half* pl = po.planes + std::uint64_t(blockIdx.y) * 4 * po.rows * k + ((kk / 16) * po.rows + row) * 64 +
                    (kk % 16);
-      pl[0] = rh;
-      pl[16] = __float2half_rn(xr - __half2float(rh));
-      pl[32] = ih;
-      pl[48] = __float2half_rn(xi - __half2float(ih));
+      pl[0] = __low2half(hi);
+      pl[16] = __low2half(lo);
+      pl[32] = __high2half(hi);
+      pl[48] = __high2half(lo);
       if ((threadIdx.x & 31) == 0)
         po.exps[std::uint64_t(blockIdx.y) * po.rows * (k / 32) + row * (k / 32) + kk / 32] = e;
     }
