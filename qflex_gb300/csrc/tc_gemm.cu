@@ -230,6 +230,82 @@ __device__ __forceinline__ void mbar_arrive(std::uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+// ---- Cluster (CTA pair) helpers ------------------------------------------------
+
+__device__ __forceinline__ std::uint32_t cluster_rank() {
+  std::uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// Shared::cluster address of the same shared-memory offset in CTA `rank`.
+__device__ __forceinline__ std::uint32_t peer_addr(const void* p, std::uint32_t rank) {
+  std::uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_test_cluster(std::uint64_t* bar, std::uint32_t parity) {
+  std::uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_cluster(std::uint64_t* bar, std::uint32_t parity, volatile int* abort_flag,
+                                                  int* err, int code) {
+  const unsigned long long t0 = now_ns();
+  while (!mbar_test_cluster(bar, parity)) {
+    if (*abort_flag) return false;
+    if (now_ns() - t0 > WAIT_NS) {
+      *abort_flag = 1;
+      atomicExch(err, code);
+      return false;
+    }
+  }
+  return true;
+}
+__device__ __forceinline__ void mbar_arrive_remote(std::uint32_t cluster_addr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
+}
+// TMA load into this CTA's shared memory that completes on a barrier of
+// either CTA of the pair (`bar` is a shared::cluster address).
+__device__ __forceinline__ void tma_load_4d_pair(const CUtensorMap* map, std::uint32_t bar, void* dst, int c0, int c1,
+                                                 int c2, int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+      "%4, %5}], [%6];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<std::uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void umma_tf32_pair(std::uint32_t d_tmem, std::uint64_t a, std::uint64_t b,
+                                               std::uint32_t idesc, std::uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+// Commit of the issuing thread's MMAs, arriving on `bar` in both CTAs.
+__device__ __forceinline__ void umma_commit_pair(std::uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "h"(std::uint16_t(3))
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_f16_pair(std::uint32_t d_tmem, std::uint64_t a, std::uint64_t b,
+                                              std::uint32_t idesc, std::uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
 // The single-CTA kernel body, persistent: CTA b takes output tiles b,
 // b + gridDim.x, ... (grouped raster, batch entries after each other), and
 // its producer, MMA issuer and epilogue run through the tiles on shared
@@ -241,7 +317,19 @@ __device__ __forceinline__ void mbar_arrive(std::uint64_t* bar) {
 // them. KIND_BF16 operands have
 // six planes per k-step: b0, b1 of re and im in a 128-byte row (map_a /
 // map_b) and b2 of re and im in a 64-byte row (map_a2 / map_b2).
-template <int KIND>
+//
+// PAIR (3xFP16 only; a cluster of two CTAs, cta_group::2): a tile is 256
+// rows x 128 complex columns. CTA r holds rows m0 + 128 r .. + 127 of A and
+// the B rows of its half of the two N = 256 operands -- CTA 0 Br and -Bi,
+// CTA 1 Bi and Br, so that (Br; Bi) and (-Bi; Br) are split across the pair
+// at the same shared-memory offsets -- and one M = 256 MMA issued by CTA 0
+// writes each CTA's 128 rows into that CTA's TMEM. Per SM and k-step that is
+// 32 KB of operands instead of 40 KB, and half the MMA instructions.
+// Synchronisation: both CTAs' TMA loads complete on CTA 0's full[s]; MMA
+// commits are multicast to both CTAs (empty, acc_full, mma_done); both
+// CTAs' epilogue warps arrive on CTA 0's acc_empty; cluster barriers after
+// set-up and before TMEM is released.
+template <int KIND, bool PAIR = false>
 __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const CUtensorMap* map_b,
                                                  const CUtensorMap* map_a2, const CUtensorMap* map_b2,
                                                  const CUtensorMap* map_c, bool tma_c,
@@ -251,9 +339,13 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
                                                  const int* __restrict__ exp_b, int a_blocks) {
   constexpr int KSTEP = KIND == KIND_TF32 ? 8 : 16;  // k values per plane row of 32 bytes
   constexpr int TAIL = BM * 64;                       // BF16 third-piece tile of one operand
-  constexpr int NST = KIND == KIND_BF16 ? 3 : (KIND == KIND_FP16 ? 4 : STAGES);
-  constexpr int SBYTES = KIND == KIND_BF16 ? 2 * (TILE_A + TAIL) : (KIND == KIND_FP16 ? F16_STAGE_BYTES : STAGE_BYTES);
+  constexpr int NST = KIND == KIND_BF16 ? 3 : (KIND == KIND_FP16 ? (PAIR ? 5 : 4) : STAGES);
+  constexpr int SBYTES = KIND == KIND_BF16   ? 2 * (TILE_A + TAIL)
+                         : KIND == KIND_FP16 ? (PAIR ? 4 * F16_BLOCK : F16_STAGE_BYTES)
+                                             : STAGE_BYTES;
+  constexpr int TM = PAIR ? 2 * BM : BM;  // rows of a tile
   static_assert(NST * SBYTES <= STAGES * STAGE_BYTES, "stages fit the shared memory of the launch");
+  static_assert(!PAIR || KIND == KIND_FP16, "the CTA pair is a 3xFP16 kernel");
   extern __shared__ __align__(1024) std::uint8_t smem_raw[];
   std::uint8_t* smem = reinterpret_cast<std::uint8_t*>((reinterpret_cast<std::uintptr_t>(smem_raw) + 1023) &
                                                        ~std::uintptr_t(1023));
@@ -268,7 +360,11 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int tiles_m = (m + BM - 1) / BM;
+  // Work items (tiles) of this CTA (of this pair): first, first + stride, ...
+  const std::uint32_t rank = PAIR ? cluster_rank() : 0;
+  const int first = PAIR ? blockIdx.x / 2 : blockIdx.x;
+  const int stride = PAIR ? gridDim.x / 2 : gridDim.x;
+  const int tiles_m = (m + TM - 1) / TM;
   const int tiles_n = (n + BN - 1) / BN;
   const int per_batch = tiles_m * tiles_n;
   const int total = per_batch * batches;
@@ -280,8 +376,19 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     const int per_group = 8 * tiles_n;
     const int group = r / per_group, in_group = r % per_group;
     const int group_m = min(8, tiles_m - group * 8);
-    m0 = (group * 8 + in_group % group_m) * BM;
+    m0 = (group * 8 + in_group % group_m) * TM + int(rank) * BM;
     n0 = (in_group / group_m) * BN;
+  };
+  // Waits on barriers that the other CTA of a pair (or its MMA commits) may
+  // complete use cluster scope.
+  auto wait = [&](std::uint64_t* bar, std::uint32_t parity, int code) {
+    return PAIR ? mbar_wait_cluster(bar, parity, abort_flag, err, code) : mbar_wait(bar, parity, abort_flag, err, code);
+  };
+  auto commit = [&](std::uint64_t* bar) {
+    if constexpr (PAIR)
+      umma_commit_pair(bar);
+    else
+      umma_commit(bar);
   };
   const int kblocks = (k + KSTEP - 1) / KSTEP;
   const int chunks = (kblocks + CHUNK - 1) / CHUNK;
@@ -293,32 +400,50 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], EPI_WARPS);
+      mbar_init(&acc_empty[b], PAIR ? 2 * EPI_WARPS : EPI_WARPS);
     }
     mbar_init(mma_done, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(TMEM_COLS));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    if constexpr (PAIR) {
+      asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                   "r"(TMEM_COLS));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+    } else {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                   "r"(TMEM_COLS));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
+  if constexpr (PAIR) cluster_sync();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const std::uint32_t tmem = *tmem_slot;
 
   if (warp == 0 && lane == 0) {
     // Producer: stage g % NST of the CTA-wide k-step count g.
     int g = 0;
-    for (int t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x) {
+    for (int t = first; t < total && !*abort_flag; t += stride) {
       int m0, n0, batch;
       tile_of(t, m0, n0, batch);
       for (int kb = 0; kb < kblocks; ++kb, ++g) {
         const int s = g % NST;
-        if (g >= NST && !mbar_wait(&empty[s], ((g / NST) - 1) & 1, abort_flag, err, 1)) break;
+        if (g >= NST && !wait(&empty[s], ((g / NST) - 1) & 1, 1)) break;
         std::uint8_t* st = smem + s * SBYTES;
+        if constexpr (PAIR) {
+          // This CTA's A rows (re, im) and its half of the B operands: CTA 0
+          // Br (x = 0) and -Bi (64), CTA 1 Bi (32) and Br (0).
+          if (rank == 0) mbar_expect_tx(&full[s], 2 * SBYTES);
+          const std::uint32_t bar = peer_addr(&full[s], 0);
+          tma_load_4d_pair(map_a, bar, st, 0, m0, kb, batch);
+          tma_load_4d_pair(map_a, bar, st + F16_BLOCK, 32, m0, kb, batch);
+          tma_load_4d_pair(map_b, bar, st + 2 * F16_BLOCK, rank ? 32 : 0, n0, kb, batch);
+          tma_load_4d_pair(map_b, bar, st + 3 * F16_BLOCK, rank ? 0 : 64, n0, kb, batch);
+          continue;
+        }
         mbar_expect_tx(&full[s], SBYTES);
         if constexpr (KIND == KIND_FP16) {
           // Planes x = 0 (re hi, lo), 32 (im hi, lo) and, for B, 64 (-im).
@@ -337,24 +462,25 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
         }
       }
     }
-    if (*abort_flag) {
+    if (*abort_flag && rank == 0) {
       // Let the copies already issued land before the CTA's shared memory
-      // is released (bounded as well).
+      // is released (bounded as well; a pair's copies complete on CTA 0).
       for (int q = g > NST ? g - NST : 0; q < g; ++q) {
         const unsigned long long t0 = now_ns();
         while (!mbar_test(&full[q % NST], (q / NST) & 1) && now_ns() - t0 < WAIT_NS) {
         }
       }
     }
-  } else if (warp == 1 && lane == 0) {
-    // MMA issuer. Planes in a stage: A re_hi, re_lo, im_hi, im_lo, then B.
+  } else if (warp == 1 && lane == 0 && rank == 0) {
+    // MMA issuer (of the pair: CTA 0). Planes in a stage: A re_hi, re_lo,
+    // im_hi, im_lo, then B.
     // Chunk c (CHUNK k-steps of one tile; c counts across tiles) accumulates
     // from zero into TMEM buffer c % 2; the epilogue warps add it into their
     // FP32 registers and free it.
     const std::uint32_t idp = idesc_kind<KIND>(BM, BN, false), idn = idesc_kind<KIND>(BM, BN, true);
     int g = 0, c = 0;
     bool go = true;
-    for (int t = blockIdx.x; t < total && go; t += gridDim.x) {
+    for (int t = first; t < total && go; t += stride) {
       for (int kb = 0; kb < kblocks; ++kb, ++g) {
         const int s = g % NST;
         const int buf = c & 1;
@@ -362,7 +488,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
         if (first && c >= 2) {
           // The epilogue's TMEM reads of this buffer precede the MMAs that
           // overwrite it.
-          if (!mbar_wait(&acc_empty[buf], ((c >> 1) - 1) & 1, abort_flag, err, 4)) {
+          if (!wait(&acc_empty[buf], ((c >> 1) - 1) & 1, 4)) {
             go = false;
             break;
           }
@@ -370,14 +496,30 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
         }
         // Operand stages need no fence: the TMA's complete_tx on the barrier
         // orders its shared-memory writes before the MMAs' reads.
-        if (!mbar_wait(&full[s], (g / NST) & 1, abort_flag, err, 2)) {
+        if (!wait(&full[s], (g / NST) & 1, 2)) {
           go = false;
           break;
         }
         const std::uint32_t d_re = tmem + buf * 2 * BN, d_im = d_re + BN;
         const std::uint32_t a0 = smem_u32(smem + s * SBYTES);
         const std::uint32_t acc = first ? 0u : 1u;
-        if constexpr (KIND == KIND_FP16) {
+        if constexpr (PAIR) {
+          // M = 256 over the pair; B rows (Br; Bi) at the stage's B offset
+          // and (-Bi; Br) 8 KB further, each half in its own CTA.
+          const std::uint32_t idw = idesc_f16(2 * BM, 2 * BN, false);
+          const std::uint32_t ar = a0, ai = a0 + F16_BLOCK, b1 = a0 + 2 * F16_BLOCK, b2 = a0 + 3 * F16_BLOCK;
+          const std::uint64_t arh = smem_desc_sw64(ar), arl = smem_desc_sw64(ar + 32);
+          const std::uint64_t aih = smem_desc_sw64(ai), ail = smem_desc_sw64(ai + 32);
+          const std::uint64_t b1h = smem_desc_sw64(b1), b1l = smem_desc_sw64(b1 + 32);
+          const std::uint64_t b2h = smem_desc_sw64(b2), b2l = smem_desc_sw64(b2 + 32);
+          umma_f16_pair(d_re, arh, b1l, idw, acc);
+          umma_f16_pair(d_re, arl, b1h, idw, 1);
+          umma_f16_pair(d_re, aih, b2l, idw, 1);
+          umma_f16_pair(d_re, ail, b2h, idw, 1);
+          umma_f16_pair(d_re, arh, b1h, idw, 1);
+          umma_f16_pair(d_re, aih, b2h, idw, 1);
+          (void)d_im;
+        } else if constexpr (KIND == KIND_FP16) {
           // One M = 128, N = 256 product gives C_re (columns 0..127) and
           // C_im (128..255) together: Ar against the B rows (Br; Bi) and Ai
           // against (-Bi; Br), both read from the stage's B blocks
@@ -453,14 +595,14 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
             umma<KIND>(d_im, aih, brh, idp, 1);
           }
         }
-        umma_commit(&empty[s]);
+        commit(&empty[s]);
         if (kb % CHUNK == CHUNK - 1 || kb == kblocks - 1) {
-          umma_commit(&acc_full[buf]);
+          commit(&acc_full[buf]);
           ++c;
         }
       }
     }
-    umma_commit(mma_done);
+    commit(mma_done);
   } else if (warp >= 2) {
     // Epilogue: warp w reads TMEM lanes [32 (w % 4), 32 (w % 4) + 32) and one
     // half of the tile's columns. The tensor core's FP32 accumulation rounds
@@ -472,7 +614,10 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     float2* stg = staging + (warp - 2) * 32 * 32;
     int c = 0;
     bool ok = true;
-    for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
+    // A pair's acc_empty barriers live in CTA 0.
+    const std::uint32_t drained0 = PAIR ? peer_addr(&acc_empty[0], 0) : 0u;
+    const std::uint32_t drained1 = PAIR ? peer_addr(&acc_empty[1], 0) : 0u;
+    for (int t = first; t < total && ok; t += stride) {
       int m0, n0, batch;
       tile_of(t, m0, n0, batch);
       float tre[BN / 2], tim[BN / 2];
@@ -487,7 +632,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
         const int buf = c & 1;
         const int e_blk = e_next;
         if (blocked && cc + 1 < chunks) e_next = eblk[((cc + 1) * CHUNK * KSTEP) / 32];
-        if (!mbar_wait(&acc_full[buf], (c >> 1) & 1, abort_flag, err, 3)) {
+        if (!wait(&acc_full[buf], (c >> 1) & 1, 3)) {
           ok = false;
           break;
         }
@@ -511,7 +656,12 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncwarp();
-        if (lane == 0) mbar_arrive(&acc_empty[buf]);
+        if (lane == 0) {
+          if constexpr (PAIR)
+            mbar_arrive_remote(buf ? drained1 : drained0);
+          else
+            mbar_arrive(&acc_empty[buf]);
+        }
       }
       if (!ok) break;
       // The MMA issuer already works on the next tile. The warp's 32 x 64
@@ -590,13 +740,23 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   if (warp == 1) {
-    // Release TMEM only after every MMA this CTA issued has completed (the
-    // wait is immediate unless the pipeline was abandoned).
+    // Release TMEM only after every MMA this CTA issued (or, in a pair, that
+    // read this CTA's shared memory) has completed; the wait is immediate
+    // unless the pipeline was abandoned.
     const unsigned long long t0 = now_ns();
-    while (!mbar_test(mma_done, 0) && now_ns() - t0 < WAIT_NS) {
+    while (!(PAIR ? mbar_test_cluster(mma_done, 0) : mbar_test(mma_done, 0)) && now_ns() - t0 < WAIT_NS) {
     }
+  }
+  if constexpr (PAIR) {
+    __syncthreads();
+    cluster_sync();
+  }
+  if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    if constexpr (PAIR)
+      asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    else
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
   }
 }
 
@@ -615,6 +775,16 @@ __global__ void __launch_bounds__(THREADS, 1)
                         const int* __restrict__ exp_a, const int* __restrict__ exp_b, int a_blocks) {
   cgemm_split_body<KIND_FP16>(&map_a, &map_b, nullptr, nullptr, &map_c, tma_c != 0, C, m, n, k, batches, c_batch_stride, err, CHUNK,
                               exp_a, exp_b, a_blocks);
+}
+
+// The 3xFP16 product on CTA pairs (see cgemm_split_body).
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
+    cgemm_fp16x3_pair_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                             const __grid_constant__ CUtensorMap map_c, int tma_c, float2* __restrict__ C, int m,
+                             int n, int k, int batches, std::uint64_t c_batch_stride, int* __restrict__ err,
+                             int CHUNK, const int* __restrict__ exp_a, const int* __restrict__ exp_b, int a_blocks) {
+  cgemm_split_body<KIND_FP16, true>(&map_a, &map_b, nullptr, nullptr, &map_c, tma_c != 0, C, m, n, k, batches,
+                                    c_batch_stride, err, CHUNK, exp_a, exp_b, a_blocks);
 }
 
 __global__ void __launch_bounds__(THREADS, 1)
@@ -653,72 +823,6 @@ constexpr int P_TILE_B = PBN_CTA * 128;
 constexpr int P_STAGE_BYTES = P_TILE_A + P_TILE_B;
 constexpr int P_SMEM_BYTES = P_STAGES * P_STAGE_BYTES + 1024 + 256;
 constexpr int P_GROUP = 4;  // pair-row tiles per raster group
-
-__device__ __forceinline__ std::uint32_t cluster_rank() {
-  std::uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-// Shared::cluster address of the same shared-memory offset in CTA `rank`.
-__device__ __forceinline__ std::uint32_t peer_addr(const void* p, std::uint32_t rank) {
-  std::uint32_t r;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
-  return r;
-}
-__device__ __forceinline__ void cluster_sync() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n barrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-__device__ __forceinline__ bool mbar_test_cluster(std::uint64_t* bar, std::uint32_t parity) {
-  std::uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ bool mbar_wait_cluster(std::uint64_t* bar, std::uint32_t parity, volatile int* abort_flag,
-                                                  int* err, int code) {
-  const unsigned long long t0 = now_ns();
-  while (!mbar_test_cluster(bar, parity)) {
-    if (*abort_flag) return false;
-    if (now_ns() - t0 > WAIT_NS) {
-      *abort_flag = 1;
-      atomicExch(err, code);
-      return false;
-    }
-  }
-  return true;
-}
-__device__ __forceinline__ void mbar_arrive_remote(std::uint32_t cluster_addr) {
-  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
-}
-// TMA load into this CTA's shared memory that completes on a barrier of
-// either CTA of the pair (`bar` is a shared::cluster address).
-__device__ __forceinline__ void tma_load_4d_pair(const CUtensorMap* map, std::uint32_t bar, void* dst, int c0, int c1,
-                                                 int c2, int c3) {
-  asm volatile(
-      "cp.async.bulk.tensor.4d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
-      "%4, %5}], [%6];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<std::uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
-      : "memory");
-}
-__device__ __forceinline__ void umma_tf32_pair(std::uint32_t d_tmem, std::uint64_t a, std::uint64_t b,
-                                               std::uint32_t idesc, std::uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
-}
-// Commit of the issuing thread's MMAs, arriving on `bar` in both CTAs.
-__device__ __forceinline__ void umma_commit_pair(std::uint64_t* bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-          smem_u32(bar)),
-      "h"(std::uint16_t(3))
-      : "memory");
-}
 
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
     cgemm_tf32x3_pair_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
@@ -1270,7 +1374,10 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
   std::call_once(attr, [] {
     check(cudaFuncSetAttribute(cgemm_fp16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
           "cudaFuncSetAttribute");
+    check(cudaFuncSetAttribute(cgemm_fp16x3_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
+          "cudaFuncSetAttribute");
   });
+  const bool use_pair = cfg.variant == 1 || (cfg.variant < 0 && m >= 2 * BM);
   const std::size_t kpad = (k + 15) / 16 * 16;
   const Fp16Workspace w = fp16_workspace(workspace, m, n, k, batch);
   __half* pa = static_cast<__half*>(w.a_planes);
@@ -1288,13 +1395,43 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
   }
   const CUtensorMap ma = plane_map_f16(pa, m, kpad, batch, BM, 64);
   const CUtensorMap mb = plane_map_f16(pb, n, kpad, batch, BN, 96);
-  const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
-  dim3 grid(persistent_grid(tiles * (std::size_t)batch), 1, 1);
   CUtensorMap mc;
   const int tma_c = output_map(C, m, n, batch_stride, batch, &mc) ? 1 : 0;
+  const int a_blocks = a_in_planes ? (int)(k / 32) : 0;
+  if (use_pair) {
+    // One cluster of two CTAs per pair of SMs, persistent over 256-row tiles.
+    const std::size_t tiles = ((m + 2 * BM - 1) / (2 * BM)) * ((n + BN - 1) / BN) * (std::size_t)batch;
+    // As many clusters as can be resident at once (SMs pair up within a
+    // GPC), at most one per tile.
+    static const int resident = [] {
+      cudaLaunchConfig_t lc = {};
+      lc.gridDim = dim3(2, 1, 1);
+      lc.blockDim = dim3(THREADS, 1, 1);
+      lc.dynamicSmemBytes = SMEM_BYTES;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = 2;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      lc.attrs = at;
+      lc.numAttrs = 1;
+      int v = 0;
+      if (cudaOccupancyMaxActiveClusters(&v, cgemm_fp16x3_pair_kernel, &lc) != cudaSuccess || v < 1) {
+        cudaGetLastError();
+        v = (int)persistent_grid(1u << 20) / 2;
+      }
+      return std::max(1, v);
+    }();
+    const unsigned clusters = (unsigned)std::min<std::size_t>(tiles, (std::size_t)resident);
+    cgemm_fp16x3_pair_kernel<<<2 * clusters, THREADS, SMEM_BYTES, s>>>(
+        ma, mb, mc, tma_c, C, (int)m, (int)n, (int)k, batch, batch_stride, err, cfg.chunk, ea, eb, a_blocks);
+    check(cudaGetLastError(), "cgemm_fp16x3_pair");
+    return;
+  }
+  const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
+  dim3 grid(persistent_grid(tiles * (std::size_t)batch), 1, 1);
   cgemm_fp16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, mc, tma_c, C, (int)m, (int)n, (int)k, batch,
-                                                        batch_stride, err, cfg.chunk, ea, eb,
-                                                        a_in_planes ? (int)(k / 32) : 0);
+                                                        batch_stride, err, cfg.chunk, ea, eb, a_blocks);
   check(cudaGetLastError(), "cgemm_fp16x3");
 }
 

@@ -137,12 +137,15 @@ def test_fp16x3_rows_of_any_magnitude(built_lib):
     assert np.max(err[ok]) < 2e-5, np.max(err[ok])
 
 
-@pytest.mark.parametrize("m,n,k", [(256, 128, 16), (300, 128, 64), (512, 96, 24), (1024, 256, 256)])
-def test_tf32x3_pair_kernel(built_lib, m, n, k):
-    """The CTA-pair (cta_group::2) 3xTF32 kernel, ragged shapes included."""
+@pytest.mark.parametrize("precision", [TF32X3, FP16X3], ids=["tf32x3", "fp16x3"])
+@pytest.mark.parametrize("m,n,k", [(256, 128, 16), (300, 128, 64), (512, 96, 24), (1024, 256, 256),
+                                   (128, 128, 32), (1536, 384, 1024)])
+def test_pair_kernel(built_lib, precision, m, n, k):
+    """The CTA-pair (cta_group::2) kernels, ragged shapes included (m = 128
+    leaves the odd CTA's rows outside the matrix)."""
     import torch
-    ctx = Context(0, TF32X3)
-    ctx.set_option("tc_pair", 1)
+    ctx = Context(0, precision)
+    ctx.set_tc_variant(m, n, k, 1)
     g = np.random.default_rng(m + n + k)
     A = (g.standard_normal((m, k)) + 1j * g.standard_normal((m, k))).astype(np.complex64)
     B = (g.standard_normal((k, n)) + 1j * g.standard_normal((k, n))).astype(np.complex64)

@@ -39,10 +39,12 @@ def test_tc_shapes_of_7x7_plan(built_lib):
 
 
 @pytest.mark.gpu
-def test_variants_graphs_and_batches_agree(built_lib):
+@pytest.mark.parametrize("precision", ["tf32x3", "fp16x3"])
+def test_variants_graphs_and_batches_agree(built_lib, precision):
+    from qflex_gb300 import FP16X3
     circuit, ordering, grid, initial, finals = rqc.workload("c2")
     finals = finals[:6]
-    ctx = Context(0, TF32X3)
+    ctx = Context(0, TF32X3 if precision == "tf32x3" else FP16X3)
     base = [a for _, a in ctx.evaluate_many(circuit, ordering, grid, initial, finals, 1 << 40)]
     shapes = autotune.tc_shapes(circuit, ordering, grid)
     assert shapes
@@ -102,3 +104,25 @@ def test_fused_fp16_planes_match_split(built_lib):
             want.append(qo.evaluate_circuit(inp, np.complex128, float(1 << 40))[0][1])
         assert rel_err(a, want) < 1e-5 and rel_err(b, want) < 1e-5
         assert rel_err(a, b) < 1e-5
+
+
+@pytest.mark.gpu
+def test_fp16x3_pair_matches_single_and_fp64(built_lib):
+    """The CTA-pair 3xFP16 kernel on every product of one 7x7 slice (fused
+    plane permutations included) against the single-CTA kernel and the FP64
+    oracle."""
+    from oracle import qflex_oracle as qo
+    from qflex_gb300 import FP16X3
+    circuit, grid = rqc.random_circuit(7, 7, 32, seed=0), rqc.grid_text(7, 7)
+    ordering, finals = rqc.ordering_7x7((0,), (1,)), rqc.random_bitstrings(49, 2, 9)
+    single, pair = Context(0, FP16X3), Context(0, FP16X3)
+    for m, n, k, _ in autotune.tc_shapes(circuit, ordering, grid):
+        pair.set_tc_variant(m, n, k, 1)
+    a = [x for _, x in single.evaluate_many(circuit, ordering, grid, "", finals, 1 << 40)]
+    b = [x for _, x in pair.evaluate_many(circuit, ordering, grid, "", finals, 1 << 40)]
+    want = []
+    for f in finals:
+        inp = qo.Input(qo.Circuit.loads(circuit), qo.load_ordering(ordering), qo.Grid.loads(grid), "", f)
+        want.append(qo.evaluate_circuit(inp, np.complex128, float(1 << 40))[0][1])
+    assert rel_err(b, want) < 1e-5 and rel_err(a, want) < 1e-5
+    assert rel_err(a, b) < 1e-5
