@@ -143,8 +143,9 @@ size_t qflex_gb300_last_ops(const qflex_gb300_context* ctx, double* out, size_t 
 int qflex_gb300_set_option(qflex_gb300_context* ctx, const char* name, double value);
 int qflex_gb300_get_option(const qflex_gb300_context* ctx, const char* name, double* value);
 /* Tensor-core kernel for products of shape (m, n, k), e.g. chosen by an
- * autotuner: 0 single CTA, 1 CTA pair (needs m >= 64), -1 removes the
- * override. Overrides "tc_pair" for that shape. */
+ * autotuner: 0 single CTA, 1 CTA pair (needs m >= 64), 2 single CTA with a
+ * deeper operand pipeline (3xFP16; the other precisions take 0), -1 removes
+ * the override. Overrides "tc_pair" for that shape. */
 int qflex_gb300_set_tc_variant(qflex_gb300_context* ctx, size_t m, size_t n, size_t k, int variant);
 
 /* ---- tensor-level operations on device memory (complex64, interleaved) ----

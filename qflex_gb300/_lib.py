@@ -166,6 +166,7 @@ class Context:
             self._h = None
             raise QflexGb300Error(rc, msg)
         self.device = device
+        self.precision = precision
 
     def close(self) -> None:
         if getattr(self, "_h", None):
@@ -186,6 +187,7 @@ class Context:
         if isinstance(precision, str):
             precision = PRECISIONS[precision]
         self._check(self._lib.qflex_gb300_set_precision(self._h, precision))
+        self.precision = precision
 
     def set_stream(self, stream: int) -> None:
         self._check(self._lib.qflex_gb300_set_stream(self._h, C.c_void_p(stream or None)))

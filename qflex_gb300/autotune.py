@@ -18,9 +18,15 @@ import json
 from pathlib import Path
 from typing import Dict, List, Optional, Sequence, Tuple
 
-from ._lib import TF32X3, Context
+from ._lib import FP16X3, TF32X3, Context
 
 VARIANTS = (0, 1)  # single CTA, CTA pair
+FP16_VARIANTS = (0, 1, 2)  # and the single CTA with five stages
+
+
+def variants(ctx: Context) -> Tuple[int, ...]:
+    """Kernel variants the product tuner times for the context's precision."""
+    return FP16_VARIANTS if getattr(ctx, "precision", None) == FP16X3 else VARIANTS
 
 
 def tc_eligible(m: int, n: int, k: int) -> bool:
@@ -68,7 +74,7 @@ def tune_products(ctx: Context, stream, shapes: Sequence[Tuple[int, int, int, in
     out = {}
     for m, n, k, _ in list(shapes)[:max_shapes]:
         ms = {}
-        for v in VARIANTS:
+        for v in variants(ctx):
             ctx.set_tc_variant(m, n, k, v)
             ms[v] = _time_multiply(ctx, stream, m, n, k, reps, warmup)
         best = min(ms, key=ms.get)

@@ -152,7 +152,7 @@ double Engine::get_option(const std::string& name) const {
 }
 
 void Engine::set_tc_variant(std::size_t m, std::size_t n, std::size_t k, int variant) {
-  if (variant < -1 || variant > 1) throw QFX_ERR("Tensor-core variant must be -1, 0 or 1.");
+  if (variant < -1 || variant > 2) throw QFX_ERR("Tensor-core variant must be -1, 0, 1 or 2.");
   if (variant == -1)
     tc_variant_.erase({m, n, k});
   else

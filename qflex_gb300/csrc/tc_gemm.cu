@@ -65,6 +65,11 @@ constexpr int TMEM_COLS = 4 * BN;         // two chunk buffers of (re, im)
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
 constexpr int STAGING_BYTES = 8 * 32 * 32 * 8;  // 32 x 32 complex64 per epilogue warp
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + STAGING_BYTES + 1024 + 256;
+// The deep 3xFP16 variant: five stages and a 2 KB output box per epilogue
+// warp (32 rows x 8 complex, 64-byte swizzle).
+constexpr int DEEP_STAGES = 5;
+constexpr int DEEP_STAGING_BYTES = EPI_WARPS * 2048;
+constexpr int DEEP_SMEM_BYTES = DEEP_STAGES * F16_STAGE_BYTES + DEEP_STAGING_BYTES + 1024 + 256;
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s per wait
 
 __device__ __forceinline__ std::uint32_t smem_u32(const void* p) {
@@ -329,7 +334,11 @@ __device__ __forceinline__ void umma_f16_pair(std::uint32_t d_tmem, std::uint64_
 // commits are multicast to both CTAs (empty, acc_full, mma_done); both
 // CTAs' epilogue warps arrive on CTA 0's acc_empty; cluster barriers after
 // set-up and before TMEM is released.
-template <int KIND, bool PAIR = false>
+//
+// DEEP (3xFP16 single CTA): five stages instead of four; the output leaves
+// in 2 KB boxes (32 rows x 8 complex) so that the staging area shrinks to
+// 16 KB. Needs the bulk-store output map (tma_c).
+template <int KIND, bool PAIR = false, bool DEEP = false>
 __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const CUtensorMap* map_b,
                                                  const CUtensorMap* map_a2, const CUtensorMap* map_b2,
                                                  const CUtensorMap* map_c, bool tma_c,
@@ -339,19 +348,22 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
                                                  const int* __restrict__ exp_b, int a_blocks) {
   constexpr int KSTEP = KIND == KIND_TF32 ? 8 : 16;  // k values per plane row of 32 bytes
   constexpr int TAIL = BM * 64;                       // BF16 third-piece tile of one operand
-  constexpr int NST = KIND == KIND_BF16 ? 3 : (KIND == KIND_FP16 ? (PAIR ? 5 : 4) : STAGES);
+  constexpr int NST = KIND == KIND_BF16 ? 3 : (KIND == KIND_FP16 ? (PAIR || DEEP ? 5 : 4) : STAGES);
   constexpr int SBYTES = KIND == KIND_BF16   ? 2 * (TILE_A + TAIL)
                          : KIND == KIND_FP16 ? (PAIR ? 4 * F16_BLOCK : F16_STAGE_BYTES)
                                              : STAGE_BYTES;
   constexpr int TM = PAIR ? 2 * BM : BM;  // rows of a tile
-  static_assert(NST * SBYTES <= STAGES * STAGE_BYTES, "stages fit the shared memory of the launch");
+  constexpr int STAGE_REGION = DEEP ? DEEP_STAGES * F16_STAGE_BYTES : STAGES * STAGE_BYTES;
+  constexpr int STG_BYTES = DEEP ? DEEP_STAGING_BYTES : STAGING_BYTES;
+  static_assert(NST * SBYTES <= STAGE_REGION, "stages fit the shared memory of the launch");
   static_assert(!PAIR || KIND == KIND_FP16, "the CTA pair is a 3xFP16 kernel");
+  static_assert(!DEEP || (KIND == KIND_FP16 && !PAIR), "the deep variant is a single-CTA 3xFP16 kernel");
   extern __shared__ __align__(1024) std::uint8_t smem_raw[];
   std::uint8_t* smem = reinterpret_cast<std::uint8_t*>((reinterpret_cast<std::uintptr_t>(smem_raw) + 1023) &
                                                        ~std::uintptr_t(1023));
-  // Output staging, 32 x 32 complex64 per epilogue warp (XOR-swizzled).
-  float2* staging = reinterpret_cast<float2*>(smem + STAGES * STAGE_BYTES);
-  std::uint64_t* full = reinterpret_cast<std::uint64_t*>(smem + STAGES * STAGE_BYTES + STAGING_BYTES);
+  // Output staging per epilogue warp: 32 x 32 complex64 (2 KB when DEEP).
+  float2* staging = reinterpret_cast<float2*>(smem + STAGE_REGION);
+  std::uint64_t* full = reinterpret_cast<std::uint64_t*>(smem + STAGE_REGION + STG_BYTES);
   std::uint64_t* empty = full + NST;
   std::uint64_t* acc_full = empty + NST;    // [2]: a chunk accumulator is complete
   std::uint64_t* acc_empty = acc_full + 2;  // [2]: a chunk accumulator was drained
@@ -611,7 +623,8 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     const int q = warp % 4;
     const int half = (warp - 2) / 4;
     const int row = q * 32 + lane;
-    float2* stg = staging + (warp - 2) * 32 * 32;
+    float2* stg =
+        reinterpret_cast<float2*>(reinterpret_cast<std::uint8_t*>(staging) + (warp - 2) * (STG_BYTES / EPI_WARPS));
     int c = 0;
     bool ok = true;
     // A pair's acc_empty barriers live in CTA 0.
@@ -680,7 +693,36 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
 #pragma unroll
       for (int j0 = 0; j0 < BN / 2; j0 += 32) {
         const int ebl = j0 ? eb1 : eb0;
-        if (tma_c) {
+        if constexpr (DEEP) {
+          // Four boxes of 32 rows x 8 complex per piece, 64-byte swizzle
+          // (16-byte unit u of row r at r * 64 + ((u ^ (r / 2) % 4) * 16)).
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            if (lane == 0) bulk_wait_read();
+            __syncwarp();
+#pragma unroll
+            for (int jj = 0; jj < 8; jj += 2) {
+              const int j = 8 * b + jj;
+              float2 v0 = make_float2(tre[j0 + j], tim[j0 + j]);
+              float2 v1 = make_float2(tre[j0 + j + 1], tim[j0 + j + 1]);
+              const int e0 = -(ea + __shfl_sync(0xffffffffu, ebl, j));
+              const int e1 = -(ea + __shfl_sync(0xffffffffu, ebl, j + 1));
+              v0 = make_float2(scale2(v0.x, e0), scale2(v0.y, e0));
+              v1 = make_float2(scale2(v1.x, e1), scale2(v1.y, e1));
+              const int u = jj / 2;
+              float4* dst = reinterpret_cast<float4*>(reinterpret_cast<std::uint8_t*>(stg) + lane * 64 +
+                                                      ((u ^ ((lane >> 1) & 3)) << 4));
+              *dst = make_float4(v0.x, v0.y, v1.x, v1.y);
+            }
+            fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) {
+              const int x = 2 * (n0 + half * (BN / 2) + j0 + 8 * b), y = m0 + q * 32;
+              if (y < m && x < 2 * n) tma_store_3d(map_c, stg, x, y, batch);
+              bulk_commit();
+            }
+          }
+        } else if (tma_c) {
           // Two boxes of 32 rows x 16 complex in the 128-byte swizzle (16-byte
           // unit u of row r at r * 128 + ((u ^ r % 8) * 16)), stored by TMA;
           // the staging area is rewritten once the previous boxes were read.
@@ -775,6 +817,16 @@ __global__ void __launch_bounds__(THREADS, 1)
                         const int* __restrict__ exp_a, const int* __restrict__ exp_b, int a_blocks) {
   cgemm_split_body<KIND_FP16>(&map_a, &map_b, nullptr, nullptr, &map_c, tma_c != 0, C, m, n, k, batches, c_batch_stride, err, CHUNK,
                               exp_a, exp_b, a_blocks);
+}
+
+// The 3xFP16 product with five stages (see cgemm_split_body).
+__global__ void __launch_bounds__(THREADS, 1)
+    cgemm_fp16x3_deep_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                             const __grid_constant__ CUtensorMap map_c, int tma_c, float2* __restrict__ C, int m,
+                             int n, int k, int batches, std::uint64_t c_batch_stride, int* __restrict__ err,
+                             int CHUNK, const int* __restrict__ exp_a, const int* __restrict__ exp_b, int a_blocks) {
+  cgemm_split_body<KIND_FP16, false, true>(&map_a, &map_b, nullptr, nullptr, &map_c, tma_c != 0, C, m, n, k, batches,
+                                           c_batch_stride, err, CHUNK, exp_a, exp_b, a_blocks);
 }
 
 // The 3xFP16 product on CTA pairs (see cgemm_split_body).
@@ -1232,10 +1284,12 @@ CUtensorMap plane_map_bf16(const __nv_bfloat16* base, std::uint64_t rows, std::u
 }
 
 // 3-D map over C as floats [batch][m][2n] for the epilogue's bulk stores,
-// box {32, 32, 1} (32 rows x 16 complex) in the 128-byte swizzle. False (and
-// the epilogue stores with plain instructions) when C is not 16-byte
-// aligned, n or the batch stride is odd, or QFLEX_TC_TMA_STORE=0.
-bool output_map(float2* C, std::size_t m, std::size_t n, std::uint64_t batch_stride, int batch, CUtensorMap* map) {
+// box {32, 32, 1} (32 rows x 16 complex) in the 128-byte swizzle, or with
+// `narrow` {16, 32, 1} (8 complex) in the 64-byte swizzle. False (and the
+// epilogue stores with plain instructions) when C is not 16-byte aligned, n
+// or the batch stride is odd, or QFLEX_TC_TMA_STORE=0.
+bool output_map(float2* C, std::size_t m, std::size_t n, std::uint64_t batch_stride, int batch, CUtensorMap* map,
+                bool narrow = false) {
   static const bool enabled = [] {
     const char* e = std::getenv("QFLEX_TC_TMA_STORE");
     return !(e && std::atoi(e) == 0);
@@ -1245,11 +1299,11 @@ bool output_map(float2* C, std::size_t m, std::size_t n, std::uint64_t batch_str
     return false;
   const cuuint64_t dims[3] = {2 * n, m, (cuuint64_t)batch};
   const cuuint64_t strides[2] = {n * 8, (batch > 1 ? batch_stride : m * n) * 8};
-  const cuuint32_t box[3] = {32, 32, 1};
+  const cuuint32_t box[3] = {narrow ? 16u : 32u, 32, 1};
   const cuuint32_t estr[3] = {1, 1, 1};
   return encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, C, dims, strides, box, estr,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
-                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, narrow ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 void check(cudaError_t e, const char* what) {
@@ -1299,6 +1353,8 @@ TcConfig tc_default_config() {
   // (1+32+1) plan; QFLEX_TC_PAIR=1 sends products with m >= 256 to the pair.
   if (const char* e = std::getenv("QFLEX_TC_PAIR"))
     if (std::atoi(e) == 1) c.variant = -1;
+  if (const char* e = std::getenv("QFLEX_TC_DEEP"))
+    if (std::atoi(e) == 1) c.variant = 2;
   return c;
 }
 
@@ -1376,6 +1432,9 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
           "cudaFuncSetAttribute");
     check(cudaFuncSetAttribute(cgemm_fp16x3_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
           "cudaFuncSetAttribute");
+    check(cudaFuncSetAttribute(cgemm_fp16x3_deep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               DEEP_SMEM_BYTES),
+          "cudaFuncSetAttribute");
   });
   const bool use_pair = cfg.variant == 1 || (cfg.variant < 0 && m >= 2 * BM);
   const std::size_t kpad = (k + 15) / 16 * 16;
@@ -1430,6 +1489,13 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
   }
   const std::size_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
   dim3 grid(persistent_grid(tiles * (std::size_t)batch), 1, 1);
+  CUtensorMap mcn;
+  if (cfg.variant == 2 && output_map(C, m, n, batch_stride, batch, &mcn, true)) {
+    cgemm_fp16x3_deep_kernel<<<grid, THREADS, DEEP_SMEM_BYTES, s>>>(ma, mb, mcn, 1, C, (int)m, (int)n, (int)k, batch,
+                                                                    batch_stride, err, cfg.chunk, ea, eb, a_blocks);
+    check(cudaGetLastError(), "cgemm_fp16x3_deep");
+    return;
+  }
   cgemm_fp16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, mc, tma_c, C, (int)m, (int)n, (int)k, batch,
                                                         batch_stride, err, cfg.chunk, ea, eb, a_blocks);
   check(cudaGetLastError(), "cgemm_fp16x3");

@@ -17,9 +17,11 @@ std::size_t tc_workspace_elems(std::size_t m, std::size_t n, std::size_t k);
 // Kernel choice of one product.
 struct TcConfig {
   int chunk = 2;     // k-steps (of 8) per TMEM accumulation chunk, 1..64
-  int variant = 0;   // 0: single CTA; 1: CTA pair; -1: CTA pair when m >= 256, else single
+  int variant = 0;   // 0: single CTA; 1: CTA pair; -1: CTA pair when m >= 256, else single;
+                     // 2: 3xFP16 single CTA with five stages (others: single CTA)
 };
-// Defaults: chunk from QFLEX_TC_CHUNK, variant -1 when QFLEX_TC_PAIR=1.
+// Defaults: chunk from QFLEX_TC_CHUNK, variant -1 when QFLEX_TC_PAIR=1, 2 when
+// QFLEX_TC_DEEP=1.
 TcConfig tc_default_config();
 
 // C[m,n] = A[m,k] * Bt[n,k]^T (complex64, both K-major), 3xTF32 split,

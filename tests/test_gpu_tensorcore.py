@@ -137,15 +137,17 @@ def test_fp16x3_rows_of_any_magnitude(built_lib):
     assert np.max(err[ok]) < 2e-5, np.max(err[ok])
 
 
-@pytest.mark.parametrize("precision", [TF32X3, FP16X3], ids=["tf32x3", "fp16x3"])
+@pytest.mark.parametrize("precision,variant", [(TF32X3, 1), (FP16X3, 1), (FP16X3, 2)],
+                         ids=["tf32x3_pair", "fp16x3_pair", "fp16x3_deep"])
 @pytest.mark.parametrize("m,n,k", [(256, 128, 16), (300, 128, 64), (512, 96, 24), (1024, 256, 256),
                                    (128, 128, 32), (1536, 384, 1024)])
-def test_pair_kernel(built_lib, precision, m, n, k):
-    """The CTA-pair (cta_group::2) kernels, ragged shapes included (m = 128
-    leaves the odd CTA's rows outside the matrix)."""
+def test_kernel_variant(built_lib, precision, variant, m, n, k):
+    """The CTA-pair (cta_group::2) kernels and the five-stage 3xFP16 kernel,
+    ragged shapes included (m = 128 leaves the odd CTA's rows of a pair
+    outside the matrix)."""
     import torch
     ctx = Context(0, precision)
-    ctx.set_tc_variant(m, n, k, 1)
+    ctx.set_tc_variant(m, n, k, variant)
     g = np.random.default_rng(m + n + k)
     A = (g.standard_normal((m, k)) + 1j * g.standard_normal((m, k))).astype(np.complex64)
     B = (g.standard_normal((k, n)) + 1j * g.standard_normal((k, n))).astype(np.complex64)

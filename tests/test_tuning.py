@@ -23,9 +23,10 @@ def test_options_round_trip_and_validation(built_lib):
     with pytest.raises(QflexGb300Error):
         c.get_option("no_such_option")
     c.set_tc_variant(4096, 4096, 4096, 1)
+    c.set_tc_variant(4096, 4096, 4096, 2)
     c.set_tc_variant(4096, 4096, 4096, -1)
     with pytest.raises(QflexGb300Error):
-        c.set_tc_variant(64, 64, 64, 2)
+        c.set_tc_variant(64, 64, 64, 3)
 
 
 def test_tc_shapes_of_7x7_plan(built_lib):
@@ -48,7 +49,7 @@ def test_variants_graphs_and_batches_agree(built_lib, precision):
     base = [a for _, a in ctx.evaluate_many(circuit, ordering, grid, initial, finals, 1 << 40)]
     shapes = autotune.tc_shapes(circuit, ordering, grid)
     assert shapes
-    for variant in (0, 1):
+    for variant in autotune.variants(ctx):
         for m, n, k, _ in shapes:
             ctx.set_tc_variant(m, n, k, variant)
         for _ in range(3):  # eager, captured, replayed
@@ -107,17 +108,18 @@ def test_fused_fp16_planes_match_split(built_lib):
 
 
 @pytest.mark.gpu
-def test_fp16x3_pair_matches_single_and_fp64(built_lib):
-    """The CTA-pair 3xFP16 kernel on every product of one 7x7 slice (fused
-    plane permutations included) against the single-CTA kernel and the FP64
-    oracle."""
+@pytest.mark.parametrize("variant", [1, 2], ids=["pair", "deep"])
+def test_fp16x3_variant_matches_single_and_fp64(built_lib, variant):
+    """The CTA-pair and five-stage 3xFP16 kernels on every product of one
+    7x7 slice (fused plane permutations included) against the single-CTA
+    kernel and the FP64 oracle."""
     from oracle import qflex_oracle as qo
     from qflex_gb300 import FP16X3
     circuit, grid = rqc.random_circuit(7, 7, 32, seed=0), rqc.grid_text(7, 7)
     ordering, finals = rqc.ordering_7x7((0,), (1,)), rqc.random_bitstrings(49, 2, 9)
     single, pair = Context(0, FP16X3), Context(0, FP16X3)
     for m, n, k, _ in autotune.tc_shapes(circuit, ordering, grid):
-        pair.set_tc_variant(m, n, k, 1)
+        pair.set_tc_variant(m, n, k, variant)
     a = [x for _, x in single.evaluate_many(circuit, ordering, grid, "", finals, 1 << 40)]
     b = [x for _, x in pair.evaluate_many(circuit, ordering, grid, "", finals, 1 << 40)]
     want = []
