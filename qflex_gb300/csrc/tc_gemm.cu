@@ -231,6 +231,14 @@ __device__ __forceinline__ void umma_commit(std::uint64_t* bar) {
         "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])                                            \
       : "r"(taddr))
 
+#define TMEM_LD16(taddr, r)                                                                            \
+  asm volatile(                                                                                        \
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];" \
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),          \
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),       \
+        "=r"(r[14]), "=r"(r[15])                                                                      \
+      : "r"(taddr))
+
 __device__ __forceinline__ void mbar_arrive(std::uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
@@ -654,15 +662,15 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
         const float sa = scale2(1.f, -e_blk);
         const std::uint32_t base = tmem + (std::uint32_t(q * 32) << 16) + buf * 2 * BN + half * (BN / 2);
 #pragma unroll
-        for (int j0 = 0; j0 < BN / 2; j0 += 32) {
-          // Both loads in flight before one wait: two TMEM round trips per
-          // chunk instead of four.
-          std::uint32_t vr[32], vi[32];
-          TMEM_LD32(base + j0, vr);
-          TMEM_LD32(base + BN + j0, vi);
+        for (int j0 = 0; j0 < BN / 2; j0 += 16) {
+          // 16 columns of re and of im per round trip: with the 128 running
+          // sums that keeps the epilogue within its 168 registers.
+          std::uint32_t vr[16], vi[16];
+          TMEM_LD16(base + j0, vr);
+          TMEM_LD16(base + BN + j0, vi);
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
+          for (int j = 0; j < 16; ++j) {
             tre[j0 + j] = fmaf(__uint_as_float(vr[j]), sa, tre[j0 + j]);
             tim[j0 + j] = fmaf(__uint_as_float(vi[j]), sa, tim[j0 + j]);
           }
