@@ -101,6 +101,7 @@ __device__ __forceinline__ bool mbar_test(std::uint64_t* bar, std::uint32_t pari
 // within WAIT_NS or another warp of the CTA has already given up.
 __device__ __forceinline__ bool mbar_wait(std::uint64_t* bar, std::uint32_t parity, volatile int* abort_flag,
                                           int* err, int code) {
+  if (mbar_test(bar, parity)) return true;  // the common case reads no timer
   const unsigned long long t0 = now_ns();
   while (!mbar_test(bar, parity)) {
     if (*abort_flag) return false;
@@ -271,6 +272,7 @@ __device__ __forceinline__ bool mbar_test_cluster(std::uint64_t* bar, std::uint3
 }
 __device__ __forceinline__ bool mbar_wait_cluster(std::uint64_t* bar, std::uint32_t parity, volatile int* abort_flag,
                                                   int* err, int code) {
+  if (mbar_test_cluster(bar, parity)) return true;
   const unsigned long long t0 = now_ns();
   while (!mbar_test_cluster(bar, parity)) {
     if (*abort_flag) return false;
@@ -498,6 +500,17 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     // from zero into TMEM buffer c % 2; the epilogue warps add it into their
     // FP32 registers and free it.
     const std::uint32_t idp = idesc_kind<KIND>(BM, BN, false), idn = idesc_kind<KIND>(BM, BN, true);
+    // 3xFP16 stage-0 descriptors: A re hi, lo, A im hi, lo, B (-im) hi, lo,
+    // B re hi, lo (B re and B im are the 256 rows (Br; Bi)).
+    std::uint64_t f16d[8];
+    {
+      const std::uint32_t s0 = smem_u32(smem);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const std::uint32_t blk = i < 4 ? std::uint32_t(i / 2) : std::uint32_t(2 + (i - 4) / 2);
+        f16d[i] = smem_desc_sw64(s0 + blk * F16_BLOCK + (i % 2) * 32);
+      }
+    }
     int g = 0, c = 0;
     bool go = true;
     for (int t = first; t < total && go; t += stride) {
@@ -545,11 +558,12 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
           // against (-Bi; Br), both read from the stage's B blocks
           // (-Bi, Br, Bi). Six MMAs per k-step, small terms first.
           const std::uint32_t idw = idesc_f16(BM, 2 * BN, false);
-          const std::uint32_t ar = a0, ai = a0 + F16_BLOCK, bn = a0 + 2 * F16_BLOCK, br = a0 + 3 * F16_BLOCK;
-          const std::uint64_t arh = smem_desc_sw64(ar), arl = smem_desc_sw64(ar + 32);
-          const std::uint64_t aih = smem_desc_sw64(ai), ail = smem_desc_sw64(ai + 32);
-          const std::uint64_t b1h = smem_desc_sw64(br), b1l = smem_desc_sw64(br + 32);
-          const std::uint64_t b2h = smem_desc_sw64(bn), b2l = smem_desc_sw64(bn + 32);
+          // Stage s's descriptors: stage 0's with the start address moved
+          // by s * SBYTES (the 14-bit field cannot carry: shared memory is
+          // below 256 KB).
+          const std::uint64_t so = std::uint64_t(s) * (SBYTES >> 4);
+          const std::uint64_t arh = f16d[0] + so, arl = f16d[1] + so, aih = f16d[2] + so, ail = f16d[3] + so;
+          const std::uint64_t b2h = f16d[4] + so, b2l = f16d[5] + so, b1h = f16d[6] + so, b1l = f16d[7] + so;
           umma<KIND>(d_re, arh, b1l, idw, acc);
           umma<KIND>(d_re, arl, b1h, idw, 1);
           umma<KIND>(d_re, aih, b2l, idw, 1);
