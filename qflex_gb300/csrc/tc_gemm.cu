@@ -446,14 +446,14 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
   const std::uint32_t tmem = *tmem_slot;
 
   if (warp == 0 && lane == 0) {
-    // Producer: stage g % NST of the CTA-wide k-step count g.
-    int g = 0;
+    // Producer: stage s (phase ph) of the CTA-wide k-step count g.
+    int g = 0, s = 0;
+    std::uint32_t ph = 0;
     for (int t = first; t < total && !*abort_flag; t += stride) {
       int m0, n0, batch;
       tile_of(t, m0, n0, batch);
-      for (int kb = 0; kb < kblocks; ++kb, ++g) {
-        const int s = g % NST;
-        if (g >= NST && !wait(&empty[s], ((g / NST) - 1) & 1, 1)) break;
+      for (int kb = 0; kb < kblocks; ++kb) {
+        if (g >= NST && !wait(&empty[s], ph ^ 1u, 1)) break;
         std::uint8_t* st = smem + s * SBYTES;
         if constexpr (PAIR) {
           // This CTA's A rows (re, im) and its half of the B operands: CTA 0
@@ -464,23 +464,28 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
           tma_load_4d_pair(map_a, bar, st + F16_BLOCK, 32, m0, kb, batch);
           tma_load_4d_pair(map_b, bar, st + 2 * F16_BLOCK, rank ? 32 : 0, n0, kb, batch);
           tma_load_4d_pair(map_b, bar, st + 3 * F16_BLOCK, rank ? 0 : 64, n0, kb, batch);
-          continue;
-        }
-        mbar_expect_tx(&full[s], SBYTES);
-        if constexpr (KIND == KIND_FP16) {
-          // Planes x = 0 (re hi, lo), 32 (im hi, lo) and, for B, 64 (-im).
-          tma_load_4d(map_a, &full[s], st, 0, m0, kb, batch);
-          tma_load_4d(map_a, &full[s], st + F16_BLOCK, 32, m0, kb, batch);
-          tma_load_4d(map_b, &full[s], st + 2 * F16_BLOCK, 64, n0, kb, batch);
-          tma_load_4d(map_b, &full[s], st + 3 * F16_BLOCK, 0, n0, kb, batch);
-          tma_load_4d(map_b, &full[s], st + 4 * F16_BLOCK, 32, n0, kb, batch);
         } else {
-          tma_load_4d(map_a, &full[s], st, 0, m0, kb, batch);
-          tma_load_4d(map_b, &full[s], st + TILE_A, 0, n0, kb, batch);
+          mbar_expect_tx(&full[s], SBYTES);
+          if constexpr (KIND == KIND_FP16) {
+            // Planes x = 0 (re hi, lo), 32 (im hi, lo) and, for B, 64 (-im).
+            tma_load_4d(map_a, &full[s], st, 0, m0, kb, batch);
+            tma_load_4d(map_a, &full[s], st + F16_BLOCK, 32, m0, kb, batch);
+            tma_load_4d(map_b, &full[s], st + 2 * F16_BLOCK, 64, n0, kb, batch);
+            tma_load_4d(map_b, &full[s], st + 3 * F16_BLOCK, 0, n0, kb, batch);
+            tma_load_4d(map_b, &full[s], st + 4 * F16_BLOCK, 32, n0, kb, batch);
+          } else {
+            tma_load_4d(map_a, &full[s], st, 0, m0, kb, batch);
+            tma_load_4d(map_b, &full[s], st + TILE_A, 0, n0, kb, batch);
+          }
+          if constexpr (KIND == KIND_BF16) {
+            tma_load_4d(map_a2, &full[s], st + 2 * TILE_A, 0, m0, kb, batch);
+            tma_load_4d(map_b2, &full[s], st + 2 * TILE_A + TAIL, 0, n0, kb, batch);
+          }
         }
-        if constexpr (KIND == KIND_BF16) {
-          tma_load_4d(map_a2, &full[s], st + 2 * TILE_A, 0, m0, kb, batch);
-          tma_load_4d(map_b2, &full[s], st + 2 * TILE_A + TAIL, 0, n0, kb, batch);
+        ++g;
+        if (++s == NST) {
+          s = 0;
+          ph ^= 1u;
         }
       }
     }
@@ -511,13 +516,16 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
         f16d[i] = smem_desc_sw64(s0 + blk * F16_BLOCK + (i % 2) * 32);
       }
     }
-    int g = 0, c = 0;
+    // Stage s with phase bit ph, k-step kc of chunk c: counters, not
+    // divisions, since this thread's instruction stream paces the MMAs.
+    int s = 0, c = 0, kc = 0;
+    std::uint32_t ph = 0;
     bool go = true;
     for (int t = first; t < total && go; t += stride) {
-      for (int kb = 0; kb < kblocks; ++kb, ++g) {
-        const int s = g % NST;
+      kc = 0;
+      for (int kb = 0; kb < kblocks; ++kb) {
         const int buf = c & 1;
-        const bool first = kb % CHUNK == 0;
+        const bool first = kc == 0;
         if (first && c >= 2) {
           // The epilogue's TMEM reads of this buffer precede the MMAs that
           // overwrite it.
@@ -529,7 +537,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
         }
         // Operand stages need no fence: the TMA's complete_tx on the barrier
         // orders its shared-memory writes before the MMAs' reads.
-        if (!wait(&full[s], (g / NST) & 1, 2)) {
+        if (!wait(&full[s], ph, 2)) {
           go = false;
           break;
         }
@@ -630,9 +638,14 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
           }
         }
         commit(&empty[s]);
-        if (kb % CHUNK == CHUNK - 1 || kb == kblocks - 1) {
+        if (++kc == CHUNK || kb == kblocks - 1) {
           commit(&acc_full[buf]);
           ++c;
+          kc = 0;
+        }
+        if (++s == NST) {
+          s = 0;
+          ph ^= 1;
         }
       }
     }
