@@ -192,6 +192,31 @@ __device__ __forceinline__ void umma_f16(std::uint32_t d_tmem, std::uint64_t a, 
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
       "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
 }
+// One k-step of the 3xFP16 product (six M = 128, N = 256 MMAs, small terms
+// first) in one instruction block. The stage's eight shared-memory
+// descriptors share their high word `hi` and differ in the low word from
+// `lo` (A re hi) by fixed offsets in 16-byte units: A re lo +2, A im +512,
+// +514, B -im +1024, +1026, B re +1536, +1538 (blocks of 8 KB, lo planes
+// 32 bytes into the rows). `acc` = 0 starts the accumulator.
+__device__ __forceinline__ void umma_f16_kstep(std::uint32_t d, std::uint32_t lo, std::uint32_t hi,
+                                               std::uint32_t idesc, std::uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p0, p1;\n .reg .b32 l1, l2, l3, l4, l5, l6, l7;\n"
+      " .reg .b64 arh, arl, aih, ail, b2h, b2l, b1h, b1l;\n"
+      " setp.ne.b32 p0, %4, 0;\n setp.eq.b32 p1, %4, %4;\n"
+      " add.u32 l1, %1, 2;\n add.u32 l2, %1, 512;\n add.u32 l3, %1, 514;\n add.u32 l4, %1, 1024;\n"
+      " add.u32 l5, %1, 1026;\n add.u32 l6, %1, 1536;\n add.u32 l7, %1, 1538;\n"
+      " mov.b64 arh, {%1, %2};\n mov.b64 arl, {l1, %2};\n mov.b64 aih, {l2, %2};\n mov.b64 ail, {l3, %2};\n"
+      " mov.b64 b2h, {l4, %2};\n mov.b64 b2l, {l5, %2};\n mov.b64 b1h, {l6, %2};\n mov.b64 b1l, {l7, %2};\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], arh, b1l, %3, p0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], arl, b1h, %3, p1;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], aih, b2l, %3, p1;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], ail, b2h, %3, p1;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], arh, b1h, %3, p1;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], aih, b2h, %3, p1;\n}\n" ::"r"(d),
+      "r"(lo), "r"(hi), "r"(idesc), "r"(acc));
+}
+
 // Operand kinds of the single-CTA kernel: 3xTF32 planes (8 values of 4
 // bytes per plane and k-step) or 3xFP16 planes (16 values of 2 bytes, rows
 // scaled by powers of two).
@@ -505,17 +530,11 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     // from zero into TMEM buffer c % 2; the epilogue warps add it into their
     // FP32 registers and free it.
     const std::uint32_t idp = idesc_kind<KIND>(BM, BN, false), idn = idesc_kind<KIND>(BM, BN, true);
-    // 3xFP16 stage-0 descriptors: A re hi, lo, A im hi, lo, B (-im) hi, lo,
-    // B re hi, lo (B re and B im are the 256 rows (Br; Bi)).
-    std::uint64_t f16d[8];
-    {
-      const std::uint32_t s0 = smem_u32(smem);
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const std::uint32_t blk = i < 4 ? std::uint32_t(i / 2) : std::uint32_t(2 + (i - 4) / 2);
-        f16d[i] = smem_desc_sw64(s0 + blk * F16_BLOCK + (i % 2) * 32);
-      }
-    }
+    // 3xFP16: descriptor of stage 0's A re hi plane; the stage's others
+    // follow at fixed offsets (umma_f16_kstep), stage s at + s SBYTES / 16.
+    const std::uint64_t f16d0 = smem_desc_sw64(smem_u32(smem));
+    const std::uint32_t f16_hi = std::uint32_t(f16d0 >> 32);
+    std::uint32_t f16_lo = std::uint32_t(f16d0);
     // Stage s with phase bit ph, k-step kc of chunk c: counters, not
     // divisions, since this thread's instruction stream paces the MMAs.
     int s = 0, c = 0, kc = 0;
@@ -565,19 +584,10 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
           // C_im (128..255) together: Ar against the B rows (Br; Bi) and Ai
           // against (-Bi; Br), both read from the stage's B blocks
           // (-Bi, Br, Bi). Six MMAs per k-step, small terms first.
-          const std::uint32_t idw = idesc_f16(BM, 2 * BN, false);
           // Stage s's descriptors: stage 0's with the start address moved
           // by s * SBYTES (the 14-bit field cannot carry: shared memory is
           // below 256 KB).
-          const std::uint64_t so = std::uint64_t(s) * (SBYTES >> 4);
-          const std::uint64_t arh = f16d[0] + so, arl = f16d[1] + so, aih = f16d[2] + so, ail = f16d[3] + so;
-          const std::uint64_t b2h = f16d[4] + so, b2l = f16d[5] + so, b1h = f16d[6] + so, b1l = f16d[7] + so;
-          umma<KIND>(d_re, arh, b1l, idw, acc);
-          umma<KIND>(d_re, arl, b1h, idw, 1);
-          umma<KIND>(d_re, aih, b2l, idw, 1);
-          umma<KIND>(d_re, ail, b2h, idw, 1);
-          umma<KIND>(d_re, arh, b1h, idw, 1);
-          umma<KIND>(d_re, aih, b2h, idw, 1);
+          umma_f16_kstep(d_re, f16_lo, f16_hi, idesc_f16(BM, 2 * BN, false), acc);
           (void)d_im;
         } else {
           const std::uint32_t b0 = a0 + TILE_A;
@@ -643,9 +653,11 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
           ++c;
           kc = 0;
         }
+        f16_lo += SBYTES >> 4;
         if (++s == NST) {
           s = 0;
           ph ^= 1;
+          f16_lo -= NST * (SBYTES >> 4);
         }
       }
     }
