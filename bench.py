@@ -39,7 +39,9 @@ WORKLOAD = "c3"
 FP32_PEAK_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12  # TFLOP/s, FP32 CUDA-core FMA
 # DRAM bytes (read + write) of one launch of the dominant product, from ncu
 # captures summarised in profiles/.
-TRAFFIC = {("tf32x3", 4096, 4096, 4096): 2.322e9, ("fp16x3", 4096, 4096, 4096): 0.991e9}
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one product kernel
+# launch of this shape with batch 1 (profiles/tc_*_4096.md).
+TRAFFIC = {("tf32x3", 4096, 4096, 4096): 2.322e9, ("fp16x3", 4096, 4096, 4096): 1.270e9}
 
 
 def parse():
@@ -179,8 +181,35 @@ def config(args):
             "l2": "inputs larger than L2 (1.1 GB HBM arena per output string)"}
 
 
+def dominant_product(ctx, circuit, ordering, grid, initial, strings):
+    """The product shape with the most device time in one profiled pass of
+    the benchmark step (CUDA events around every launch on the context's
+    stream): (m, n, k, launches, batch, mean ms per launch incl. the
+    B-operand split, share of the pass)."""
+    import collections
+    ctx.set_profiling(True)
+    try:
+        ctx.evaluate_many(circuit, ordering, grid, initial, strings, 1 << 40)
+        ops = ctx.ops()
+    finally:
+        ctx.set_profiling(False)
+    agg = collections.defaultdict(lambda: [0, 0.0, 1])
+    total = 0.0
+    for r in ops:
+        total += r[7]
+        if int(r[0]) in (1, 2):
+            a = agg[(int(r[1]), int(r[2]), int(r[3]))]
+            a[0] += 1
+            a[1] += r[7]
+            a[2] = int(r[6])
+    (m, n, k), (cnt, ms, batch) = max(agg.items(), key=lambda kv: kv[1][1])
+    return m, n, k, cnt, batch, ms / cnt, ms / total
+
+
 def dominant_kernel_time(ctx, torch, m, n, k, reps=5):
-    """CUDA-event time of the dominant product shape on the context's stream."""
+    """CUDA-event time of one product of shape (m, n, k) through the public
+    multiply entry (both operands split, B transposed) on the context's
+    stream."""
     A = torch.randn((m, k), dtype=torch.complex64, device="cuda")
     B = torch.randn((k, n), dtype=torch.complex64, device="cuda")
     C = torch.empty((m, n), dtype=torch.complex64, device="cuda")
@@ -330,10 +359,10 @@ def main():
         # Accuracy of this path, then the plain FP32 CUDA-core path timed on
         # the same workload for the ratio the metric asks for.
         line["accuracy"] = accuracy_vs_fp64(ctx, circuit, ordering, grid, initial)
-        shapes = sorted(ctx.shapes(), key=lambda x: -x[0] * x[1] * x[2] * x[3])
-        m, n, k, _ = shapes[0]
-        kt_ms = dominant_kernel_time(ctx, torch, m, n, k)
-        achieved = 8.0 * m * n * k / (kt_ms / 1e3) / 1e12
+        m, n, k, launches, pbatch, op_ms, share = dominant_product(ctx, circuit, ordering, grid, initial,
+                                                                   strings(0))
+        achieved = 8.0 * m * n * k * pbatch / (op_ms / 1e3) / 1e12
+        single = 8.0 * m * n * k / (dominant_kernel_time(ctx, torch, m, n, k) / 1e3) / 1e12
         pk = peaks()
         if args.precision == "fp32":
             line["roofline"] = {
@@ -341,7 +370,9 @@ def main():
                 "peak": FP32_PEAK_NOMINAL, "unit": "TFLOP/s", "frac": achieved / FP32_PEAK_NOMINAL,
                 "peak_source": "nominal FP32 CUDA-core FMA rate (152 SMs x 128 lanes x 2 x 2.07 GHz); "
                                "the measured peaks hold no FP32 CUDA-core figure",
-                "traffic": None, "timing": "CUDA events, dominant shape, 5 launches"}
+                "traffic": None, "timing": f"CUDA events around each of the {launches} launches of this shape "
+                                           f"(batch {pbatch}) in one profiled pass of the step; "
+                                           f"{100 * share:.0f}% of the pass"}
         else:
             # Split products: 4 real products x 3 terms (3xTF32, 3xFP16) or
             # x 6 terms (BF16x3) = 12 or 24 MMAs of 2mnk per 8mnk of
@@ -353,13 +384,17 @@ def main():
             terms = 6.0 if args.precision == "bf16x3" else 3.0
             src = "measured bf16 dense burst" if "bf16_tflops" in pk else "fallback 1.9 PFLOP/s bf16"
             line["roofline"] = {
-                "bound": "tensor", "kernel": f"cgemm_{args.precision} ({m},{n},{k}) incl. plane splits",
+                "bound": "tensor", "kernel": f"cgemm_{args.precision} ({m},{n},{k}) x{pbatch} incl. B-plane split",
                 "achieved": terms * achieved, "achieved_algorithmic": achieved, "peak": mma_peak,
                 "unit": "TFLOP/s (16-bit MMA)" if fp16 else "TFLOP/s (TF32 MMA)", "frac": terms * achieved / mma_peak,
                 "peak_source": src + (" (MEASURED_PEAKS.json)" if "bf16_tflops" in pk else "") + ("" if fp16 else " / 2"),
-                "traffic": TRAFFIC.get((args.precision, m, n, k)),
-                "traffic_source": "ncu dram__bytes_read+write of one launch of this shape (profiles/)",
-                "timing": "CUDA events on the context stream, dominant shape, 5 launches"}
+                "traffic": (TRAFFIC[(args.precision, m, n, k)] * pbatch
+                            if (args.precision, m, n, k) in TRAFFIC else None),
+                "traffic_source": "ncu dram__bytes_read+write of one batch-1 launch of this shape (profiles/), "
+                                  "times the batch: each product of the batch reads its own operands",
+                "timing": f"CUDA events around each of the {launches} launches of this shape (batch {pbatch}) "
+                          f"in one profiled pass of the step on the context stream; {100 * share:.0f}% of the pass",
+                "single_product_tflops": single}
             # The other paths on the same workload, one step each (after a
             # warm-up step): the plain FP32 CUDA-core path the metric compares
             # against, and the other split-precision mode.
