@@ -134,6 +134,7 @@ __device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, const void*
 }
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
@@ -770,35 +771,38 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
             }
           }
         } else if (tma_c) {
-          // Two boxes of 32 rows x 16 complex in the 128-byte swizzle (16-byte
-          // unit u of row r at r * 128 + ((u ^ r % 8) * 16)), stored by TMA;
-          // the staging area is rewritten once the previous boxes were read.
-          if (lane == 0) bulk_wait_read();
-          __syncwarp();
+          // Boxes of 32 rows x 16 complex in the 128-byte swizzle (16-byte
+          // unit u of row r at r * 128 + ((u ^ r % 8) * 16)), stored by TMA
+          // from two 4 KB slots in turn; a slot is rewritten once the box
+          // stored from it two boxes earlier was read (one commit group per
+          // box, at most one other still reading).
 #pragma unroll
-          for (int j = 0; j < 32; j += 2) {
-            float2 v0 = make_float2(tre[j0 + j], tim[j0 + j]);
-            float2 v1 = make_float2(tre[j0 + j + 1], tim[j0 + j + 1]);
-            if (KIND == KIND_FP16) {
-              const int e0 = -(ea + __shfl_sync(0xffffffffu, ebl, j));
-              const int e1 = -(ea + __shfl_sync(0xffffffffu, ebl, j + 1));
-              v0 = make_float2(scale2(v0.x, e0), scale2(v0.y, e0));
-              v1 = make_float2(scale2(v1.x, e1), scale2(v1.y, e1));
+          for (int b = 0; b < 2; ++b) {
+            std::uint8_t* slot = reinterpret_cast<std::uint8_t*>(stg) + b * 4096;
+            if (lane == 0) bulk_wait_read1();
+            __syncwarp();
+#pragma unroll
+            for (int jj = 0; jj < 16; jj += 2) {
+              const int j = 16 * b + jj;
+              float2 v0 = make_float2(tre[j0 + j], tim[j0 + j]);
+              float2 v1 = make_float2(tre[j0 + j + 1], tim[j0 + j + 1]);
+              if (KIND == KIND_FP16) {
+                const int e0 = -(ea + __shfl_sync(0xffffffffu, ebl, j));
+                const int e1 = -(ea + __shfl_sync(0xffffffffu, ebl, j + 1));
+                v0 = make_float2(scale2(v0.x, e0), scale2(v0.y, e0));
+                v1 = make_float2(scale2(v1.x, e1), scale2(v1.y, e1));
+              }
+              const int u = jj / 2;
+              float4* dst = reinterpret_cast<float4*>(slot + lane * 128 + ((u ^ (lane & 7)) << 4));
+              *dst = make_float4(v0.x, v0.y, v1.x, v1.y);
             }
-            const int u = (j % 16) / 2;
-            float4* dst = reinterpret_cast<float4*>(reinterpret_cast<std::uint8_t*>(stg) + (j / 16) * 4096 +
-                                                    lane * 128 + ((u ^ (lane & 7)) << 4));
-            *dst = make_float4(v0.x, v0.y, v1.x, v1.y);
-          }
-          fence_proxy_async();
-          __syncwarp();
-          if (lane == 0) {
-            const int x = 2 * (n0 + half * (BN / 2) + j0), y = m0 + q * 32;
-            if (y < m) {
-              if (x < 2 * n) tma_store_3d(map_c, stg, x, y, batch);
-              if (x + 32 < 2 * n) tma_store_3d(map_c, reinterpret_cast<std::uint8_t*>(stg) + 4096, x + 32, y, batch);
+            fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) {
+              const int x = 2 * (n0 + half * (BN / 2) + j0 + 16 * b), y = m0 + q * 32;
+              if (y < m && x < 2 * n) tma_store_3d(map_c, slot, x, y, batch);
+              bulk_commit();
             }
-            bulk_commit();
           }
         } else {
           // Element (r, j) of the piece sits at r * 32 + (j ^ r); the warp
