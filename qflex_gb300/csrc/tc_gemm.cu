@@ -731,12 +731,36 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
       // 3xFP16 scale exponents: the row's (unless A's blocks were applied
       // per chunk) and, per piece, that of column j0 + lane.
       int ea = 0, eb0 = 0, eb1 = 0;
+      bool fast = true;
       if (KIND == KIND_FP16) {
         ea = (a_blocks == 0 && m0 + row < m) ? exp_a[std::uint64_t(batch) * m + m0 + row] : 0;
         const int* eb = exp_b + std::uint64_t(batch) * n + n0 + half * (BN / 2);
         eb0 = lane < ncols ? eb[lane] : 0;
         eb1 = 32 + lane < ncols ? eb[32 + lane] : 0;
+        // When every scale 2^-(ea + eb) of the warp's block is a normal
+        // float, each element takes one multiply by it (exact unless the
+        // result leaves the normal range, then rounded as ldexpf rounds).
+        const int lo = __reduce_min_sync(0xffffffffu, ea) + __reduce_min_sync(0xffffffffu, min(eb0, eb1));
+        const int hi = __reduce_max_sync(0xffffffffu, ea) + __reduce_max_sync(0xffffffffu, max(eb0, eb1));
+        fast = hi <= 126 && lo >= -127;
       }
+      // Output element (re, im) of column j of the piece: scaled by
+      // 2^-(ea + eb_j), eb_j held by lane j. Otherwise by two powers of two
+      // 2^e1 2^e2 (e1 + e2 = e, each clamped to the normal range): the first
+      // multiply is exact whenever the result is normal, and an exponent
+      // beyond +-252 only arises for results far outside the float range.
+      auto out = [&](float re, float im, int ebl, int j) -> float2 {
+        if (KIND != KIND_FP16) return make_float2(re, im);
+        const int ebj = __shfl_sync(0xffffffffu, ebl, j);
+        if (fast) {
+          const float sc = __uint_as_float(std::uint32_t(127 - ea - ebj) << 23);
+          return make_float2(re * sc, im * sc);
+        }
+        const int e = -(ea + ebj), e1 = min(max(e >> 1, -126), 127), e2 = min(max(e - e1, -126), 127);
+        const float s1 = __uint_as_float(std::uint32_t(e1 + 127) << 23);
+        const float s2 = __uint_as_float(std::uint32_t(e2 + 127) << 23);
+        return make_float2(re * s1 * s2, im * s1 * s2);
+      };
       float2* cb = C + std::uint64_t(batch) * c_batch_stride;
 #pragma unroll
       for (int j0 = 0; j0 < BN / 2; j0 += 32) {
@@ -751,12 +775,8 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
 #pragma unroll
             for (int jj = 0; jj < 8; jj += 2) {
               const int j = 8 * b + jj;
-              float2 v0 = make_float2(tre[j0 + j], tim[j0 + j]);
-              float2 v1 = make_float2(tre[j0 + j + 1], tim[j0 + j + 1]);
-              const int e0 = -(ea + __shfl_sync(0xffffffffu, ebl, j));
-              const int e1 = -(ea + __shfl_sync(0xffffffffu, ebl, j + 1));
-              v0 = make_float2(scale2(v0.x, e0), scale2(v0.y, e0));
-              v1 = make_float2(scale2(v1.x, e1), scale2(v1.y, e1));
+              const float2 v0 = out(tre[j0 + j], tim[j0 + j], ebl, j);
+              const float2 v1 = out(tre[j0 + j + 1], tim[j0 + j + 1], ebl, j + 1);
               const int u = jj / 2;
               float4* dst = reinterpret_cast<float4*>(reinterpret_cast<std::uint8_t*>(stg) + lane * 64 +
                                                       ((u ^ ((lane >> 1) & 3)) << 4));
@@ -784,14 +804,8 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
 #pragma unroll
             for (int jj = 0; jj < 16; jj += 2) {
               const int j = 16 * b + jj;
-              float2 v0 = make_float2(tre[j0 + j], tim[j0 + j]);
-              float2 v1 = make_float2(tre[j0 + j + 1], tim[j0 + j + 1]);
-              if (KIND == KIND_FP16) {
-                const int e0 = -(ea + __shfl_sync(0xffffffffu, ebl, j));
-                const int e1 = -(ea + __shfl_sync(0xffffffffu, ebl, j + 1));
-                v0 = make_float2(scale2(v0.x, e0), scale2(v0.y, e0));
-                v1 = make_float2(scale2(v1.x, e1), scale2(v1.y, e1));
-              }
+              const float2 v0 = out(tre[j0 + j], tim[j0 + j], ebl, j);
+              const float2 v1 = out(tre[j0 + j + 1], tim[j0 + j + 1], ebl, j + 1);
               const int u = jj / 2;
               float4* dst = reinterpret_cast<float4*>(slot + lane * 128 + ((u ^ (lane & 7)) << 4));
               *dst = make_float4(v0.x, v0.y, v1.x, v1.y);
@@ -809,12 +823,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
           // stores whole 32-column row pieces.
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
-            float2 v = make_float2(tre[j0 + j], tim[j0 + j]);
-            if (KIND == KIND_FP16) {
-              const int e = -(ea + __shfl_sync(0xffffffffu, ebl, j));
-              v = make_float2(scale2(v.x, e), scale2(v.y, e));
-            }
-            stg[lane * 32 + (j ^ lane)] = v;
+            stg[lane * 32 + (j ^ lane)] = out(tre[j0 + j], tim[j0 + j], ebl, j);
           }
           __syncwarp();
           for (int r = 0; r < 32; ++r) {
