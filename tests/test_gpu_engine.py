@@ -75,7 +75,9 @@ SHAPES = [(1, 1, 1), (2, 4, 2), (16, 1, 2), (1, 4, 4), (3, 5, 7), (64, 64, 64), 
           (256, 16, 16), (16, 256, 16), (4096, 1, 64), (1, 4096, 64), (1, 1, 100000),
           (2, 3, 50000), (513, 257, 129), (1024, 16, 16), (8, 300, 9),
           # vector times matrix with long k: the split-k row-reading kernel
-          (1, 64, 1 << 16), (1, 2, 8192), (1, 200, 5000), (1, 256, 4096)]
+          (1, 64, 1 << 16), (1, 2, 8192), (1, 200, 5000), (1, 256, 4096),
+          # n = 16 with short rows: the row-per-thread kernel (ragged last block)
+          (128, 16, 16), (300, 16, 7), (65536, 16, 16), (1000, 16, 32), (129, 16, 1)]
 
 
 @pytest.mark.parametrize("m,n,k", SHAPES)
@@ -95,9 +97,10 @@ def test_multiply_matches_fp64(gpu_ctx, m, n, k):
     assert np.max(np.abs(dC.cpu().numpy() - want)) / np.sqrt(k) < tol
 
 
-def test_multiply_batched(gpu_ctx):
+@pytest.mark.parametrize("m,n,k", [(64, 48, 40), (300, 16, 16)])
+def test_multiply_batched(gpu_ctx, m, n, k):
     torch = _torch()
-    m, n, k, batch = 64, 48, 40, 5
+    batch = 5
     stride = m * k + k * n + m * n
     g = np.random.default_rng(5)
     buf = (g.standard_normal((batch, stride)) + 1j * g.standard_normal((batch, stride))).astype(np.complex64)
