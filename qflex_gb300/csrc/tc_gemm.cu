@@ -21,14 +21,18 @@
 // warps add chunk c - 1 into FP32 registers with round-to-nearest. The
 // result is as accurate as FP32 CUDA-core arithmetic.
 //
-// Kernel structure (one 128 x 128 output tile per CTA, 320 threads):
-//   warp 0      TMA producer: one 4-D box per operand and stage brings all
-//               four planes of one k-step (8 values per plane side by side
-//               = one 128-byte row per tile row, 128-byte swizzle)
-//   warp 1      TMEM allocation and the single MMA-issuing thread
+// Kernel structure (persistent, one CTA per SM taking 128 x 128 complex
+// output tiles in turn, 320 threads):
+//   warp 0      TMA producer: 4-D boxes bring one k-step of the operands'
+//               planes per stage (3xTF32 / BF16x3: all planes of a row in
+//               one 128-byte row; 3xFP16: five 64-byte blocks, see below)
+//   warp 1      TMEM allocation and the single MMA-issuing thread, whose
+//               instruction stream paces the tensor core: its loops count
+//               stages and chunks instead of dividing, and a barrier test
+//               reads no timer unless it must wait
 //   warps 2..9  epilogue: warp w owns TMEM lanes 32 (w % 4) .. + 31 and one
 //               half of the columns; it drains every chunk into registers
-//               and finally writes complex64
+//               and finally stores complex64 tiles with TMA bulk stores
 // Every mbarrier wait is bounded in time; on expiry the CTA records an
 // error code, stops issuing work, waits (bounded) for what it issued and
 // frees its TMEM before returning.
@@ -916,7 +920,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 // N = 128 issued by the even CTA reads both CTAs' tiles and writes each
 // CTA's 128 rows into that CTA's TMEM. Per k-step an SM now reads 6 KB of
 // operands per MMA (its A rows and half of B) instead of 8 KB, and TMA
-// writes 24 KB instead of 32 KB, which is what bounded the single-CTA tile.
+// writes 24 KB instead of 32 KB. Measured slower than the single-CTA tile
+// on the products of the 7x7 plan; opt-in per shape.
 //
 // Synchronisation across the pair:
 //   * both CTAs' TMA loads complete on the even CTA's full[s] barrier, which
