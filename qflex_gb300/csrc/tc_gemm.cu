@@ -25,7 +25,8 @@
 // output tiles in turn, 320 threads):
 //   warp 0      TMA producer: 4-D boxes bring one k-step of the operands'
 //               planes per stage (3xTF32 / BF16x3: all planes of a row in
-//               one 128-byte row; 3xFP16: five 64-byte blocks, see below)
+//               one 128-byte row; 3xFP16: A's 128-byte rows and three
+//               blocks of 64-byte B rows, see umma_f16_kstep)
 //   warp 1      TMEM allocation and the single MMA-issuing thread, whose
 //               instruction stream paces the tensor core: its loops count
 //               stages and chunks instead of dividing, and a barrier test
@@ -60,8 +61,10 @@ constexpr int STAGES = 5;
 constexpr int TILE_A = BM * 128;
 constexpr int TILE_B = BN * 128;
 constexpr int STAGE_BYTES = TILE_A + TILE_B;
-// 3xFP16 stage: five blocks of 128 rows x 64 bytes (one k-step of hi and lo
-// in the 64-byte swizzle): A re, A im, B -im, B re, B im.
+// 3xFP16 stage: 40 KB of five 8 KB blocks, one k-step: A's 128 rows of 128
+// bytes (re hi, lo, im hi, lo; 128-byte swizzle) fill the first two, then B
+// rows of 64 bytes (hi, lo; 64-byte swizzle) of -im, re and im. (The CTA
+// pair loads A's re and im halves as separate 64-byte blocks instead.)
 constexpr int F16_BLOCK = BM * 64;
 constexpr int F16_STAGE_BYTES = 5 * F16_BLOCK;
 constexpr int EPI_WARPS = 8;
@@ -198,28 +201,29 @@ __device__ __forceinline__ void umma_f16(std::uint32_t d_tmem, std::uint64_t a, 
       "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
 }
 // One k-step of the 3xFP16 product (six M = 128, N = 256 MMAs, small terms
-// first) in one instruction block. The stage's eight shared-memory
-// descriptors share their high word `hi` and differ in the low word from
-// `lo` (A re hi) by fixed offsets in 16-byte units: A re lo +2, A im +512,
-// +514, B -im +1024, +1026, B re +1536, +1538 (blocks of 8 KB, lo planes
-// 32 bytes into the rows). `acc` = 0 starts the accumulator.
-__device__ __forceinline__ void umma_f16_kstep(std::uint32_t d, std::uint32_t lo, std::uint32_t hi,
-                                               std::uint32_t idesc, std::uint32_t acc) {
+// first) in one instruction block. The stage is A's 16 KB block of 128-byte
+// rows (re hi, lo, im hi, lo; 128-byte swizzle, high descriptor word `hia`)
+// and B's 8 KB blocks of 64-byte rows (-im, re, im; 64-byte swizzle, `hib`).
+// The low descriptor words differ from `lo` (A re hi) by fixed offsets in
+// 16-byte units: A re lo +2, A im hi +4, lo +6; B -im +1024, +1026, B re
+// +1536, +1538. `acc` = 0 starts the accumulator.
+__device__ __forceinline__ void umma_f16_kstep(std::uint32_t d, std::uint32_t lo, std::uint32_t hia,
+                                               std::uint32_t hib, std::uint32_t idesc, std::uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p0, p1;\n .reg .b32 l1, l2, l3, l4, l5, l6, l7;\n"
       " .reg .b64 arh, arl, aih, ail, b2h, b2l, b1h, b1l;\n"
-      " setp.ne.b32 p0, %4, 0;\n setp.eq.b32 p1, %4, %4;\n"
-      " add.u32 l1, %1, 2;\n add.u32 l2, %1, 512;\n add.u32 l3, %1, 514;\n add.u32 l4, %1, 1024;\n"
+      " setp.ne.b32 p0, %5, 0;\n setp.eq.b32 p1, %5, %5;\n"
+      " add.u32 l1, %1, 2;\n add.u32 l2, %1, 4;\n add.u32 l3, %1, 6;\n add.u32 l4, %1, 1024;\n"
       " add.u32 l5, %1, 1026;\n add.u32 l6, %1, 1536;\n add.u32 l7, %1, 1538;\n"
       " mov.b64 arh, {%1, %2};\n mov.b64 arl, {l1, %2};\n mov.b64 aih, {l2, %2};\n mov.b64 ail, {l3, %2};\n"
-      " mov.b64 b2h, {l4, %2};\n mov.b64 b2l, {l5, %2};\n mov.b64 b1h, {l6, %2};\n mov.b64 b1l, {l7, %2};\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], arh, b1l, %3, p0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], arl, b1h, %3, p1;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], aih, b2l, %3, p1;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], ail, b2h, %3, p1;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], arh, b1h, %3, p1;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], aih, b2h, %3, p1;\n}\n" ::"r"(d),
-      "r"(lo), "r"(hi), "r"(idesc), "r"(acc));
+      " mov.b64 b2h, {l4, %3};\n mov.b64 b2l, {l5, %3};\n mov.b64 b1h, {l6, %3};\n mov.b64 b1l, {l7, %3};\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], arh, b1l, %4, p0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], arl, b1h, %4, p1;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], aih, b2l, %4, p1;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], ail, b2h, %4, p1;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], arh, b1h, %4, p1;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], aih, b2h, %4, p1;\n}\n" ::"r"(d),
+      "r"(lo), "r"(hia), "r"(hib), "r"(idesc), "r"(acc));
 }
 
 // Operand kinds of the single-CTA kernel: 3xTF32 planes (8 values of 4
@@ -497,9 +501,9 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
         } else {
           mbar_expect_tx(&full[s], SBYTES);
           if constexpr (KIND == KIND_FP16) {
-            // Planes x = 0 (re hi, lo), 32 (im hi, lo) and, for B, 64 (-im).
+            // A: one box of whole 128-byte rows (16 KB); B: planes x = 64
+            // (-im), 0 (re) and 32 (im), hi and lo each.
             tma_load_4d(map_a, &full[s], st, 0, m0, kb, batch);
-            tma_load_4d(map_a, &full[s], st + F16_BLOCK, 32, m0, kb, batch);
             tma_load_4d(map_b, &full[s], st + 2 * F16_BLOCK, 64, n0, kb, batch);
             tma_load_4d(map_b, &full[s], st + 3 * F16_BLOCK, 0, n0, kb, batch);
             tma_load_4d(map_b, &full[s], st + 4 * F16_BLOCK, 32, n0, kb, batch);
@@ -537,8 +541,9 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     const std::uint32_t idp = idesc_kind<KIND>(BM, BN, false), idn = idesc_kind<KIND>(BM, BN, true);
     // 3xFP16: descriptor of stage 0's A re hi plane; the stage's others
     // follow at fixed offsets (umma_f16_kstep), stage s at + s SBYTES / 16.
-    const std::uint64_t f16d0 = smem_desc_sw64(smem_u32(smem));
-    const std::uint32_t f16_hi = std::uint32_t(f16d0 >> 32);
+    const std::uint64_t f16d0 = smem_desc_sw128(smem_u32(smem));
+    const std::uint32_t f16_hia = std::uint32_t(f16d0 >> 32);
+    const std::uint32_t f16_hib = std::uint32_t(smem_desc_sw64(smem_u32(smem)) >> 32);
     std::uint32_t f16_lo = std::uint32_t(f16d0);
     // Stage s with phase bit ph, k-step kc of chunk c: counters, not
     // divisions, since this thread's instruction stream paces the MMAs.
@@ -592,7 +597,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
           // Stage s's descriptors: stage 0's with the start address moved
           // by s * SBYTES (the 14-bit field cannot carry: shared memory is
           // below 256 KB).
-          umma_f16_kstep(d_re, f16_lo, f16_hi, idesc_f16(BM, 2 * BN, false), acc);
+          umma_f16_kstep(d_re, f16_lo, f16_hia, f16_hib, idesc_f16(BM, 2 * BN, false), acc);
           (void)d_im;
         } else {
           const std::uint32_t b0 = a0 + TILE_A;
@@ -1305,20 +1310,22 @@ CUtensorMap plane_map(const float* base, std::uint64_t rows, std::uint64_t kpad,
 }
 
 // 4-D map over FP16 planes laid out [batch][kpad / 16][rows][row_halves]
-// (64: re hi, lo, im hi, lo; 96: also -im hi, lo), box {32, box_rows, 1, 1}:
-// the hi and lo planes of one part as 64-byte rows, 64-byte swizzle; the
-// part is chosen by the box's x coordinate (0, 32, 64).
+// (64: re hi, lo, im hi, lo; 96: also -im hi, lo). Box {32, box_rows, 1, 1}:
+// the hi and lo planes of one part as 64-byte rows, 64-byte swizzle, the
+// part chosen by the box's x coordinate (0, 32, 64); or with box_inner = 64
+// whole 128-byte rows (all four planes of A) in the 128-byte swizzle.
 CUtensorMap plane_map_f16(const __half* base, std::uint64_t rows, std::uint64_t kpad, int batch, int box_rows,
-                          int row_halves) {
+                          int row_halves, int box_inner = 32) {
   CUtensorMap map;
   std::memset(&map, 0, sizeof(map));
   const std::uint64_t kb = kpad / 16, rb = std::uint64_t(row_halves) * 2;
   const cuuint64_t dims[4] = {(cuuint64_t)row_halves, rows, kb, (cuuint64_t)batch};
   const cuuint64_t strides[3] = {rb, rows * rb, kb * rows * rb};
-  const cuuint32_t box[4] = {32, (cuuint32_t)box_rows, 1, 1};
+  const cuuint32_t box[4] = {(cuuint32_t)box_inner, (cuuint32_t)box_rows, 1, 1};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 4, const_cast<__half*>(base), dims, strides, box,
-                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           box_inner == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS)
     throw std::string("ERROR (qflex_gb300: tensor cores) --> cuTensorMapEncodeTiled failed: ") +
@@ -1517,6 +1524,9 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
     split_fp16_kernel<<<gb, 256, 0, s>>>(Bt, pb, eb, n, k, kpad, bt_stride, 6);
     check(cudaGetLastError(), "split_fp16");
   }
+  // A: whole 128-byte rows for the single-CTA kernels, re / im halves for
+  // the pair; B: 64-byte halves.
+  const CUtensorMap ma_rows = plane_map_f16(pa, m, kpad, batch, BM, 64, 64);
   const CUtensorMap ma = plane_map_f16(pa, m, kpad, batch, BM, 64);
   const CUtensorMap mb = plane_map_f16(pb, n, kpad, batch, BN, 96);
   CUtensorMap mc;
@@ -1556,12 +1566,12 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
   dim3 grid(persistent_grid(tiles * (std::size_t)batch), 1, 1);
   CUtensorMap mcn;
   if (cfg.variant == 2 && output_map(C, m, n, batch_stride, batch, &mcn, true)) {
-    cgemm_fp16x3_deep_kernel<<<grid, THREADS, DEEP_SMEM_BYTES, s>>>(ma, mb, mcn, 1, C, (int)m, (int)n, (int)k, batch,
-                                                                    batch_stride, err, cfg.chunk, ea, eb, a_blocks);
+    cgemm_fp16x3_deep_kernel<<<grid, THREADS, DEEP_SMEM_BYTES, s>>>(
+        ma_rows, mb, mcn, 1, C, (int)m, (int)n, (int)k, batch, batch_stride, err, cfg.chunk, ea, eb, a_blocks);
     check(cudaGetLastError(), "cgemm_fp16x3_deep");
     return;
   }
-  cgemm_fp16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma, mb, mc, tma_c, C, (int)m, (int)n, (int)k, batch,
+  cgemm_fp16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma_rows, mb, mc, tma_c, C, (int)m, (int)n, (int)k, batch,
                                                         batch_stride, err, cfg.chunk, ea, eb, a_blocks);
   check(cudaGetLastError(), "cgemm_fp16x3");
 }
