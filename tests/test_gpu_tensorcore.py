@@ -27,7 +27,7 @@ def tc_ctx(built_lib, request):
                                    (300, 128, 64), (128, 1024, 40), (4096, 256, 256), (256, 64, 16),
                                    (512, 96, 24), (768, 200, 100), (2048, 2048, 2048), (256, 97, 64),
                                    (200, 131, 48)])
-def test_tf32x3_multiply(tc_ctx, m, n, k):
+def test_split_multiply(tc_ctx, m, n, k):
     import torch
     g = np.random.default_rng(m + 7 * n + 13 * k)
     A = (g.standard_normal((m, k)) + 1j * g.standard_normal((m, k))).astype(np.complex64)
@@ -51,7 +51,7 @@ ENGINE_CASES = ["c1_4x5_d16", "rect4x4_cut_terminal", "c2_6x6_d24_partial_cut", 
 
 
 @pytest.mark.parametrize("name", ENGINE_CASES)
-def test_tf32x3_engine_close_to_reference(tc_ctx, ref_cases, name):
+def test_split_engine_close_to_reference(tc_ctx, ref_cases, name):
     """Against the reference's complex<float> results. The split path
     evaluates the gates from double constants; the reference's float gate
     constants alone move a 7x7 amplitude by ~7e-6, so the bound there is
@@ -68,7 +68,7 @@ def test_tf32x3_engine_close_to_reference(tc_ctx, ref_cases, name):
 
 
 @pytest.mark.parametrize("name", ["c1_4x5_d16", "rect4x4_cut_terminal", "fsim_3x4_off", "c2_6x6_d24_partial_cut"])
-def test_tf32x3_engine_matches_fp64(tc_ctx, ref_cases, name):
+def test_split_engine_matches_fp64(tc_ctx, ref_cases, name):
     case = ref_cases[name]
     runs = case["runs"][:3]
     out = tc_ctx.evaluate_many(case["circuit"], case["ordering"], case["grid"], case["initial"],
@@ -81,7 +81,7 @@ def test_tf32x3_engine_matches_fp64(tc_ctx, ref_cases, name):
     assert rel_err([a for _, a in out], want) < TOL, name
 
 
-def test_tf32x3_7x7_within_1e5_of_fp64(tc_ctx):
+def test_split_7x7_within_1e5_of_fp64(tc_ctx):
     """7x7 (1+32+1), benchmark ordering with one value per cut: per-amplitude
     relative error against the FP64 oracle below 1e-5."""
     c = rqc.random_circuit(7, 7, 32, seed=0)
@@ -95,7 +95,7 @@ def test_tf32x3_7x7_within_1e5_of_fp64(tc_ctx):
         assert abs(a - want) <= TOL * abs(want), (f, a, want)
 
 
-def test_tf32x3_plan_uses_tensor_cores(tc_ctx, ref_cases):
+def test_split_plan_uses_tensor_cores(tc_ctx, ref_cases):
     case = ref_cases["c3_7x7_d32_one_slice"]
     tc_ctx.evaluate(case["circuit"], case["ordering"], case["grid"], "", "", 1 << 40)
     plan = Context(-1, TF32X3)
@@ -103,7 +103,7 @@ def test_tf32x3_plan_uses_tensor_cores(tc_ctx, ref_cases):
     assert plan.gemms() == [tuple(g) for g in case["runs"][0]["gemms"]]
 
 
-def test_tf32x3_vs_fp64_oracle_c1(tc_ctx):
+def test_split_vs_fp64_oracle_c1(tc_ctx):
     c, o, g, ini, fins = rqc.workload("c1", seed=8)
     out = tc_ctx.evaluate_many(c, o, g, ini, fins[:4])
     want = []
