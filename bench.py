@@ -55,6 +55,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-autotune", action="store_true",
                    help="skip the tensor-core kernel / strings-per-pass autotuning before warm-up")
+    p.add_argument("--cpu-sample", type=int, default=0, metavar="SLICES",
+                   help="only time the CPU oracle on SLICES cut slices and print that as JSON")
     return p.parse_args()
 
 
@@ -283,9 +285,23 @@ def shared_region(ctx, torch, stream, circuit, grid, initial, finals, strings=2,
             "note": "not the headline: strings share 43 of 49 bits"}
 
 
+def cpu_sample_single_thread(slices: int = 1):
+    """cpu_sample on one core: a child process with one OpenBLAS / OpenMP
+    thread (the thread count is fixed when numpy loads its BLAS)."""
+    import subprocess
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--cpu-sample", str(slices)], env=env,
+                         capture_output=True, text=True, check=True, timeout=600)
+    return json.loads(out.stdout.strip().splitlines()[-1])
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.cpu_sample:
+        dt, v, desc, cores = cpu_sample(slices=args.cpu_sample)
+        print(json.dumps({"seconds": dt, "value": v, "sample": desc}))
+        return
     if args.impl == "reference":
         run_reference(args, rank)
         return
@@ -415,6 +431,9 @@ def main():
             dt, v, desc, cores = cpu_sample(slices=4)
             line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                     "sample": desc}
+            one = cpu_sample_single_thread(1)
+            line["cpu_baseline"]["single_thread"] = {"value": one["value"], "unit": UNIT, "cores": 1,
+                                                     "sample": one["sample"]}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
