@@ -1,6 +1,7 @@
 """Micro-benchmarks of the engine's kernels through the C ABI.
 
     python -m qflex_gb300.kernel_bench gemm --m 4096 --n 4096 --k 4096 --precision tf32x3
+    python -m qflex_gb300.kernel_bench gemm --m 65536 --n 256 --k 256 --precision fp16x3 --batch 8
     python -m qflex_gb300.kernel_bench permute --bits 24 --seed 1
 
 Times launches with CUDA events on the context's stream (after warm-up) and
@@ -40,15 +41,21 @@ def _time(torch, stream, fn, reps: int, warmup: int) -> float:
     return e0.elapsed_time(e1) / reps
 
 
-def gemm(m: int, n: int, k: int, precision: str, reps: int, warmup: int) -> dict:
+def gemm(m: int, n: int, k: int, precision: str, reps: int, warmup: int, batch: int = 1,
+         variant: int = -1) -> dict:
+    """`batch` products per launch (operands of entry b at b * (m k + k n +
+    m n) complex); `variant` >= 0 sets the tensor-core kernel variant of the
+    shape (qflex_gb300_set_tc_variant)."""
     torch, ctx, stream = _setup(precision)
-    A = torch.randn((m, k), dtype=torch.complex64, device="cuda")
-    B = torch.randn((k, n), dtype=torch.complex64, device="cuda")
-    C = torch.empty((m, n), dtype=torch.complex64, device="cuda")
-    ms = _time(torch, stream, lambda: ctx.multiply(A.data_ptr(), B.data_ptr(), C.data_ptr(), m, n, k),
-               reps, warmup)
-    return {"kernel": "multiply", "precision": precision, "m": m, "n": n, "k": k, "ms": ms,
-            "tflops": 8.0 * m * n * k / (ms / 1e3) / 1e12}
+    if variant >= 0:
+        ctx.set_tc_variant(m, n, k, variant)
+    stride = m * k + k * n + m * n
+    buf = torch.randn((batch, stride), dtype=torch.complex64, device="cuda")
+    base = buf.data_ptr()
+    a, b, c = base, base + 8 * m * k, base + 8 * (m * k + k * n)
+    ms = _time(torch, stream, lambda: ctx.multiply(a, b, c, m, n, k, batch, stride), reps, warmup)
+    return {"kernel": "multiply", "precision": precision, "m": m, "n": n, "k": k, "batch": batch,
+            "variant": variant, "ms": ms, "tflops": 8.0 * m * n * k * batch / (ms / 1e3) / 1e12}
 
 
 def permute(bits: int, seed: int, reps: int, warmup: int) -> dict:
@@ -71,6 +78,9 @@ def main() -> None:
     g.add_argument("--n", type=int, default=4096)
     g.add_argument("--k", type=int, default=4096)
     g.add_argument("--precision", default="tf32x3")
+    g.add_argument("--batch", type=int, default=1)
+    g.add_argument("--variant", type=int, default=-1,
+                   help="tensor-core kernel variant: 0 single CTA, 1 CTA pair, 2 five stages")
     q = sub.add_parser("permute")
     q.add_argument("--bits", type=int, default=24)
     q.add_argument("--seed", type=int, default=1)
@@ -79,7 +89,7 @@ def main() -> None:
         s.add_argument("--warmup", type=int, default=2)
     a = p.parse_args()
     if a.what == "gemm":
-        out = gemm(a.m, a.n, a.k, a.precision, a.reps, a.warmup)
+        out = gemm(a.m, a.n, a.k, a.precision, a.reps, a.warmup, a.batch, a.variant)
     else:
         out = permute(a.bits, a.seed, a.reps, a.warmup)
     print(json.dumps(out))
