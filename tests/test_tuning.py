@@ -128,3 +128,13 @@ def test_fp16x3_variant_matches_single_and_fp64(built_lib, variant):
         want.append(qo.evaluate_circuit(inp, np.complex128, float(1 << 40))[0][1])
     assert rel_err(b, want) < 1e-5 and rel_err(a, want) < 1e-5
     assert rel_err(a, b) < 1e-5
+
+
+def test_variant_sets_per_precision(built_lib):
+    """The product tuner times the five-stage kernel only for 3xFP16."""
+    from qflex_gb300 import FP16X3
+    assert autotune.variants(Context(-1, FP16X3)) == (0, 1, 2)
+    assert autotune.variants(Context(-1, TF32X3)) == (0, 1)
+    c = Context(-1, TF32X3)
+    c.set_precision("fp16x3")
+    assert autotune.variants(c) == (0, 1, 2)
