@@ -128,49 +128,94 @@ def peaks():
         return {}
 
 
-def cpu_sample(slices: int = 1):
-    """The oracle port (numpy over OpenBLAS, the reference's algorithm) on
-    `slices` of the benchmark workload's 16 cut slices x one output string.
-    Returns (seconds, amplitudes/s extrapolated by the planned flop ratio,
-    sample description, cores)."""
-    import numpy as np
+REF_BIN = ROOT / "oracle" / "_ref" / "qflex_ref"
 
-    from oracle import qflex_oracle as qo
-    from qflex_gb300 import Context, rqc
-    circuit, ordering, grid, initial, finals = rqc.workload(WORKLOAD)
-    one = rqc.ordering_7x7((0,), tuple(range(slices)))
-    plan = Context(-1)
-    plan.evaluate(circuit, ordering, grid, initial, finals[0], 1 << 40)
-    flop_full = plan.stats()["gemm_flop"]
-    plan.evaluate(circuit, one, grid, initial, finals[0], 1 << 40)
-    flop_one = plan.stats()["gemm_flop"]
-    inp = qo.Input(qo.Circuit.loads(circuit), qo.load_ordering(one), qo.Grid.loads(grid), initial, finals[0])
-    t0 = time.perf_counter()
-    qo.evaluate_circuit(inp, np.complex64, float(1 << 40))
-    dt = time.perf_counter() - t0
-    value = (flop_one / flop_full) / dt
-    desc = (f"{slices} of the 16 cut slices x 1 string of the 7x7 (1+32+1) workload ({flop_one:.3e} flop, "
-            f"{dt:.2f} s), scaled to the 16-slice amplitude ({flop_full:.3e} flop) by the flop ratio")
-    return dt, value, desc, os.cpu_count()
+
+def _rqc():
+    """qflex_gb300/rqc.py loaded on its own (it needs numpy only), so that the
+    CPU baseline legs build the workload without importing the product
+    package or loading its library."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("qflex_rqc_standalone", ROOT / "qflex_gb300" / "rqc.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def reference_binary():
+    """The unmodified reference build (oracle/Makefile), if this machine has
+    one that runs."""
+    return REF_BIN if REF_BIN.exists() and os.access(REF_BIN, os.X_OK) else None
+
+
+def cpu_sample(slices: int = 4, threads: int = 0, reps: int = 1):
+    """The reference's CPU path on `slices` of the benchmark workload's 16 cut
+    slices x one output string, `reps` times: the unmodified reference
+    (oracle/_ref/qflex_ref, OpenBLAS + OpenMP) when it is built here, else
+    the oracle port (numpy over OpenBLAS). `threads` (0: all host cores)
+    sets the OpenBLAS / OpenMP thread count. Each run is scaled to the
+    16-slice amplitude by the planned flop ratio (constants committed with
+    the workload, pinned by a test against the reference's own product log).
+    Returns (seconds per run, amplitudes/s per run, description, threads, kind)."""
+    rqc = _rqc()
+    circuit, _, grid, initial, finals = rqc.workload(WORKLOAD)
+    sample = rqc.ordering_7x7((0,), tuple(range(slices)))
+    flop_sample, flop_full = rqc.C3_GEMM_FLOP[slices], rqc.C3_GEMM_FLOP[16]
+    threads = threads or os.cpu_count()
+    ref = reference_binary()
+    secs = []
+    if ref is not None:
+        import tempfile
+        with tempfile.TemporaryDirectory() as d:
+            paths = []
+            for name, text in (("circuit", circuit), ("ordering", sample), ("grid", grid)):
+                path = Path(d) / name
+                path.write_text(text)
+                paths.append(str(path))
+            env = dict(os.environ, OMP_NUM_THREADS=str(threads), OPENBLAS_NUM_THREADS=str(threads))
+            out = subprocess.run([str(ref), "threads", str(threads), "time", str(reps), "eval", *paths, initial,
+                                  finals[0], "64GB"], env=env, capture_output=True, text=True, check=True,
+                                 timeout=3600)
+            secs = [float(ln.split()[1]) for ln in out.stdout.splitlines() if ln.startswith("SECONDS ")]
+        kind, what = "reference", "the unmodified reference (oracle/_ref/qflex_ref, OpenBLAS + OpenMP)"
+    else:
+        if threads != os.cpu_count():
+            raise RuntimeError("the oracle port takes its thread count from the environment of a new process")
+        import numpy as np
+
+        from oracle import qflex_oracle as qo
+        inp = qo.Input(qo.Circuit.loads(circuit), qo.load_ordering(sample), qo.Grid.loads(grid), initial,
+                       finals[0])
+        for _ in range(reps):
+            inp.initial_state, inp.final_state = initial, finals[0]
+            t0 = time.perf_counter()
+            qo.evaluate_circuit(inp, np.complex64, float(1 << 40))
+            secs.append(time.perf_counter() - t0)
+        kind, what = "port", "the oracle port (the reference's algorithm in numpy over OpenBLAS)"
+    values = [(flop_sample / flop_full) / dt for dt in secs]
+    desc = (f"{what} on {slices} of the 16 cut slices x 1 string of the 7x7 (1+32+1) workload "
+            f"({flop_sample:.4e} flop, {statistics.mean(secs):.2f} s per run, {threads} threads), scaled to the "
+            f"16-slice amplitude ({flop_full:.4e} flop) by the flop ratio")
+    return secs, values, desc, threads, kind
 
 
 def run_reference(args, rank):
+    """--impl reference: the reference's CPU implementation of the path on
+    this machine's host cores, rank 0 only. Warm-up steps run one cut slice,
+    timed steps four of the 16 (one process, EvaluateCircuit timed alone)."""
     if rank != 0:
         return
-    for _ in range(args.warmup):
-        cpu_sample()
-    vals = []
+    if args.warmup:
+        cpu_sample(slices=1, reps=args.warmup)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        dt, v, desc, cores = cpu_sample()
-        vals.append(v)
+    secs, vals, desc, cores, kind = cpu_sample(slices=4, reps=args.steps)
     wall = time.perf_counter() - t0
     value = statistics.mean(vals)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(secs),
+            "wall_s": wall, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
             "data": "synthetic", "config": config(args),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -227,19 +272,46 @@ def dominant_kernel_time(ctx, torch, m, n, k, reps=5):
     return e0.elapsed_time(e1) / reps
 
 
-def accuracy_vs_fp64(ctx, circuit, ordering, grid, initial):
-    """Relative error of the amplitudes of the first output strings against
-    the committed FP64 oracle values (tests/golden/c3_fp64.json)."""
-    path = ROOT / "tests" / "golden" / "c3_fp64.json"
-    if not path.exists():
+def fp64_reference():
+    """FP64-oracle amplitudes of the workload's first output strings: the
+    GPU complex128 contraction's (tests/golden/c3_fp64_gpu.json, 256
+    strings) when committed, else the CPU complex128 oracle's
+    (tests/golden/c3_fp64.json)."""
+    gpu = ROOT / "tests" / "golden" / "c3_fp64_gpu.json"
+    cpu = ROOT / "tests" / "golden" / "c3_fp64.json"
+    for path, what in ((gpu, "FP64 GPU oracle (complex128 contraction, float-float products; "
+                             "tests/golden/c3_fp64_gpu.json)"),
+                       (cpu, "FP64 CPU oracle (numpy complex128, double gate constants; tests/golden/c3_fp64.json)")):
+        if path.exists():
+            ref = json.loads(path.read_text())
+            return ref, what
+    return None, None
+
+
+def accuracy_vs_fp64(ctx, circuit, ordering, grid, batch):
+    """Per-amplitude relative error |a - a64| / |a64| of this context's
+    amplitudes against the FP64 oracle, over every string of the oracle
+    fixture, evaluated `batch` strings per call after one untimed call. The
+    calls' device time gives the path's throughput over those steps."""
+    import math
+    ref, what = fp64_reference()
+    if ref is None:
         return None
-    ref = json.loads(path.read_text())
     finals = [r["final"] for r in ref["amplitudes"]]
     want = [complex(*r["amplitude"]) for r in ref["amplitudes"]]
-    got = [a for _, a in ctx.evaluate_many(circuit, ordering, grid, ref["initial"], finals, 1 << 40)]
-    errs = [abs(a - b) / abs(b) for a, b in zip(got, want)]
-    return {"max_rel_err_vs_fp64": max(errs), "per_amplitude": [float(f"{e:.3g}") for e in errs],
-            "amplitudes": len(errs), "reference": "FP64 oracle (complex128, double gate constants)"}
+    ctx.evaluate_many(circuit, ordering, grid, ref["initial"], finals[:batch], 1 << 40)
+    got, device_ms = [], 0.0
+    for i in range(0, len(finals), batch):
+        got += [a for _, a in ctx.evaluate_many(circuit, ordering, grid, ref["initial"], finals[i:i + batch],
+                                                1 << 40)]
+        device_ms += ctx.stats()["device_ms"]
+    errs = sorted(abs(a - b) / abs(b) for a, b in zip(got, want))
+    n = len(errs)
+    return {"max_rel_err_vs_fp64": errs[-1], "median_rel_err": errs[n // 2],
+            "p99_rel_err": errs[min(n - 1, int(math.ceil(0.99 * n)) - 1)],
+            "over_1e-5": sum(e > 1e-5 for e in errs), "amplitudes": n, "reference": what,
+            "throughput": {"value": n / (device_ms / 1e3), "unit": UNIT, "steps": (n + batch - 1) // batch,
+                           "strings_per_step": batch}}
 
 
 def timed_steps(ctx, torch, stream, circuit, ordering, grid, initial, strings, first, steps):
@@ -285,22 +357,12 @@ def shared_region(ctx, torch, stream, circuit, grid, initial, finals, strings=2,
             "note": "not the headline: strings share 43 of 49 bits"}
 
 
-def cpu_sample_single_thread(slices: int = 1):
-    """cpu_sample on one core: a child process with one OpenBLAS / OpenMP
-    thread (the thread count is fixed when numpy loads its BLAS)."""
-    import subprocess
-    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
-    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--cpu-sample", str(slices)], env=env,
-                         capture_output=True, text=True, check=True, timeout=600)
-    return json.loads(out.stdout.strip().splitlines()[-1])
-
-
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.cpu_sample:
-        dt, v, desc, cores = cpu_sample(slices=args.cpu_sample)
-        print(json.dumps({"seconds": dt, "value": v, "sample": desc}))
+        secs, vals, desc, cores, kind = cpu_sample(slices=args.cpu_sample)
+        print(json.dumps({"seconds": secs[0], "value": vals[0], "sample": desc, "kind": kind}))
         return
     if args.impl == "reference":
         run_reference(args, rank)
@@ -372,9 +434,9 @@ def main():
                      "slices": st["n_leaves"]}}
 
     if rank == 0 and world == 1:
-        # Accuracy of this path, then the plain FP32 CUDA-core path timed on
-        # the same workload for the ratio the metric asks for.
-        line["accuracy"] = accuracy_vs_fp64(ctx, circuit, ordering, grid, initial)
+        # Accuracy of this path against the FP64 oracle, then the plain FP32
+        # CUDA-core path and the other split precisions on the same workload.
+        line["accuracy"] = accuracy_vs_fp64(ctx, circuit, ordering, grid, B)
         m, n, k, launches, pbatch, op_ms, share = dominant_product(ctx, circuit, ordering, grid, initial,
                                                                    strings(0))
         achieved = 8.0 * m * n * k * pbatch / (op_ms / 1e3) / 1e12
@@ -390,50 +452,62 @@ def main():
                                            f"(batch {pbatch}) in one profiled pass of the step; "
                                            f"{100 * share:.0f}% of the pass"}
         else:
-            # Split products: 4 real products x 3 terms (3xTF32, 3xFP16) or
-            # x 6 terms (BF16x3) = 12 or 24 MMAs of 2mnk per 8mnk of
-            # algorithmic work. TF32 runs at half the bf16 rate, FP16 and
-            # BF16 at the bf16 rate.
-            bf16 = pk.get("bf16_tflops", 1900.0)
+            # Algorithmic rate (8 m n k per complex product, whatever the
+            # method) against the measured bf16 dense peak; the kernel is
+            # timed inside a seconds-long step, so the sustained figure is
+            # the denominator. The split methods issue more MMA work than
+            # that: 4 real products x 3 terms (3xTF32, 3xFP16) or x 6 terms
+            # (BF16x3) per complex product, at the bf16 rate (FP16, BF16)
+            # or half of it (TF32); mma_frac is that issued rate against
+            # the same peak, and caps.tensor_method is the algorithmic
+            # ceiling the method leaves.
+            sustained = "bf16_tflops_sustained" in pk
+            peak = pk.get("bf16_tflops_sustained", 1700.0)
+            src = ("measured bf16 dense, sustained (MEASURED_PEAKS.json bf16_tflops_sustained)" if sustained
+                   else "fallback 1.7 PFLOP/s bf16 sustained")
             fp16 = args.precision in ("fp16x3", "bf16x3")
-            mma_peak = bf16 if fp16 else bf16 / 2
+            mma_peak = peak if fp16 else peak / 2
             terms = 6.0 if args.precision == "bf16x3" else 3.0
-            src = "measured bf16 dense burst" if "bf16_tflops" in pk else "fallback 1.9 PFLOP/s bf16"
+            mma_rate = terms * achieved
+            ai = 8.0 * m * n * k / (8.0 * (m * k + k * n + m * n))  # flop per byte, operands and result once
             line["roofline"] = {
                 "bound": "tensor", "kernel": f"cgemm_{args.precision} ({m},{n},{k}) x{pbatch} incl. B-plane split",
-                "achieved": terms * achieved, "achieved_algorithmic": achieved, "peak": mma_peak,
-                "unit": "TFLOP/s (16-bit MMA)" if fp16 else "TFLOP/s (TF32 MMA)", "frac": terms * achieved / mma_peak,
-                "peak_source": src + (" (MEASURED_PEAKS.json)" if "bf16_tflops" in pk else "") + ("" if fp16 else " / 2"),
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "peak_source": src,
+                "mma_achieved": mma_rate, "mma_peak": mma_peak, "mma_frac": mma_rate / mma_peak,
+                "mma_unit": "TFLOP/s (16-bit MMA)" if fp16 else "TFLOP/s (TF32 MMA)",
+                "caps": {"tensor_method": mma_peak / terms, "hbm": ai * pk.get("hbm_gbs", 6800.0) / 1e3,
+                         "unit": "TFLOP/s algorithmic"},
                 "traffic": (TRAFFIC[(args.precision, m, n, k)] * pbatch
                             if (args.precision, m, n, k) in TRAFFIC else None),
                 "traffic_source": "ncu dram__bytes_read+write of one batch-1 launch of this shape (profiles/), "
                                   "times the batch: each product of the batch reads its own operands",
+                "algorithmic_bytes": 8.0 * (m * k + k * n + m * n) * pbatch,
                 "timing": f"CUDA events around each of the {launches} launches of this shape (batch {pbatch}) "
                           f"in one profiled pass of the step on the context stream; {100 * share:.0f}% of the pass",
                 "single_product_tflops": single}
-            # The other paths on the same workload, one step each (after a
-            # warm-up step): the plain FP32 CUDA-core path the metric compares
-            # against, and the other split-precision mode.
+            # The other paths on the same workload: each runs every string of
+            # the FP64 oracle fixture, B strings per step (after one untimed
+            # step); the device time of those steps is its throughput.
             for other in [q for q in ("fp32", "tf32x3", "bf16x3", "fp16x3") if q != args.precision]:
                 fp = Context(local)
                 fp.set_precision(other)
                 fp.set_stream(stream.cuda_stream)
-                fp.evaluate_many(circuit, ordering, grid, initial, strings(0), 1 << 40)
-                f_dev, _ = timed_steps(fp, torch, stream, circuit, ordering, grid, initial, strings,
-                                       args.warmup, 1)
-                o_value = B / (f_dev / 1000.0)
-                line[f"{other}_path"] = {"value": o_value, "unit": UNIT, "steps": 1,
-                                         "speedup_of_this_path": value / o_value,
-                                         "accuracy": accuracy_vs_fp64(fp, circuit, ordering, grid, initial)}
+                acc = accuracy_vs_fp64(fp, circuit, ordering, grid, B)
+                o_value = acc["throughput"]["value"]
+                line[f"{other}_path"] = {"value": o_value, "unit": UNIT, "steps": acc["throughput"]["steps"],
+                                         "speedup_of_this_path": value / o_value, "accuracy": acc}
                 fp.close()
             line["shared_region"] = shared_region(ctx, torch, stream, circuit, grid, initial, finals)
         if not args.no_cpu_baseline:
-            dt, v, desc, cores = cpu_sample(slices=4)
-            line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+            secs, vals, desc, cores, kind = cpu_sample(slices=4)
+            line["cpu_baseline"] = {"value": vals[0], "unit": UNIT, "cores": cores, "kind": kind,
                                     "sample": desc}
-            one = cpu_sample_single_thread(1)
-            line["cpu_baseline"]["single_thread"] = {"value": one["value"], "unit": UNIT, "cores": 1,
-                                                     "sample": one["sample"]}
+            if kind == "reference":
+                # Threading helps the large products and hurts the small ones.
+                secs, vals, desc, _, _ = cpu_sample(slices=1, threads=1)
+                line["cpu_baseline"]["single_thread"] = {"value": vals[0], "unit": UNIT, "cores": 1,
+                                                         "sample": desc}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

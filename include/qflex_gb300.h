@@ -33,6 +33,11 @@ extern "C" {
 #define QFLEX_GB300_TF32X3 1 /* split 3xTF32 on tcgen05 tensor cores */
 #define QFLEX_GB300_BF16X3 2 /* split BF16x3 (six products per real product) on tcgen05 tensor cores */
 #define QFLEX_GB300_FP16X3 3 /* split 3xFP16 (rows scaled by powers of two) on tcgen05 tensor cores */
+/* The FP64 GPU oracle: the same contraction in complex128 (double gate
+ * constants, complex128 tensors in HBM, FP64 amplitude sums). The reference
+ * has no FP64 mode (its s_type is std::complex<float>, src/tensor.h:29). */
+#define QFLEX_GB300_FP64 4    /* every product with FP64 FMAs */
+#define QFLEX_GB300_FP64_FF 5 /* tiled products in float-float (~44 bits) on the FP32 pipes, rest FP64 */
 
 typedef struct qflex_gb300_context qflex_gb300_context;
 
@@ -150,6 +155,7 @@ int qflex_gb300_set_tc_variant(qflex_gb300_context* ctx, size_t m, size_t n, siz
 
 /* ---- tensor-level operations on device memory (complex64, interleaved) ----
  * Pointers are CUDA device pointers; work is queued on the context's stream.
+ * They need a complex64 precision mode (not QFLEX_GB300_FP64 / _FP64_FF).
  */
 
 /* Out-of-place index permutation: the data movement of Tensor::reorder

@@ -13,6 +13,12 @@
 //       tensor of n binary indices named i0..i(n-1) with data[p] = p,
 //       reordered to (i<perm[0]>, ...); prints the real parts.
 //   qflex_ref threads <n> eval ...   (sets the OpenBLAS thread count first)
+//   qflex_ref [threads <n>] time <reps> eval ...
+//       runs EvaluateCircuit <reps> times on the loaded input and prints
+//       "SECONDS <s>" for each run (wall time of the call alone, input
+//       loading excluded), then the amplitudes of the last run.
+#include <chrono>
+#include <complex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -28,7 +34,9 @@
 
 extern "C" void scipy_openblas_set_num_threads(int);
 
-static int do_eval(int argc, char** argv) {
+static bool timed_mode = false;
+
+static int do_eval(int argc, char** argv, int reps = 1) {
   if (argc < 7) {
     std::fprintf(stderr, "eval needs 5 arguments\n");
     return 64;
@@ -43,7 +51,19 @@ static int do_eval(int argc, char** argv) {
     if (argc > 7)
       qflex::global::memory_limit =
           qflex::utils::from_readable_memory_string(argv[7]);
-    auto amps = qflex::EvaluateCircuit(&input);
+    const std::string initial = input.initial_state, final_state = input.final_state;
+    std::vector<std::pair<std::string, std::complex<double>>> amps;
+    for (int r = 0; r < reps; ++r) {
+      // EvaluateCircuit mutates the states; every run starts from the
+      // caller's strings.
+      input.initial_state = initial;
+      input.final_state = final_state;
+      const auto t0 = std::chrono::steady_clock::now();
+      amps = qflex::EvaluateCircuit(&input);
+      const auto t1 = std::chrono::steady_clock::now();
+      if (reps > 1 || timed_mode)
+        std::printf("SECONDS %.6f\n", std::chrono::duration<double>(t1 - t0).count());
+    }
     std::printf("INITIAL %s\n", input.initial_state.c_str());
     std::printf("FINAL %s\n", input.final_state.c_str());
     for (auto& [state, a] : amps)
@@ -81,7 +101,15 @@ int main(int argc, char** argv) {
     argv += 2;
     argc -= 2;
   }
-  if (argc >= 2 && !std::strcmp(argv[1], "eval")) return do_eval(argc, argv);
+  int reps = 1;
+  if (argc >= 3 && !std::strcmp(argv[1], "time")) {
+    reps = std::atoi(argv[2]);
+    if (reps < 1) reps = 1;
+    timed_mode = true;
+    argv += 2;
+    argc -= 2;
+  }
+  if (argc >= 2 && !std::strcmp(argv[1], "eval")) return do_eval(argc, argv, reps);
   if (argc >= 3 && !std::strcmp(argv[1], "reorder"))
     return do_reorder(argc, argv);
   std::fprintf(stderr, "usage: qflex_ref [threads N] eval|reorder ...\n");

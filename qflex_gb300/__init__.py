@@ -9,7 +9,9 @@ Public surface:
   * ``rqc``: seeded random-circuit, grid and ordering generators for the
     benchmark workloads.
 """
-from ._lib import (BF16X3, FP16X3, FP32, TF32X3, Context, QflexGb300Error, load_library)  # noqa: F401
+from ._lib import (BF16X3, FP16X3, FP32, FP64, FP64_FF, TF32X3, Context, QflexGb300Error,  # noqa: F401
+                   load_library)
 from .qflex import simulate  # noqa: F401
 
-__all__ = ["Context", "QflexGb300Error", "load_library", "simulate", "FP32", "TF32X3", "BF16X3", "FP16X3"]
+__all__ = ["Context", "QflexGb300Error", "load_library", "simulate", "FP32", "TF32X3", "BF16X3", "FP16X3", "FP64",
+           "FP64_FF"]

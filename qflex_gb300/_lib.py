@@ -13,8 +13,9 @@ from typing import List, Optional, Sequence, Tuple
 LIB_PATH = Path(__file__).resolve().parent / "libqflex_gb300.so"
 
 OK, ERR_INPUT, ERR_CUDA, ERR_ARG = 0, 1, 2, 3
-FP32, TF32X3, BF16X3, FP16X3 = 0, 1, 2, 3
-PRECISIONS = {"fp32": FP32, "tf32x3": TF32X3, "bf16x3": BF16X3, "fp16x3": FP16X3}
+FP32, TF32X3, BF16X3, FP16X3, FP64, FP64_FF = 0, 1, 2, 3, 4, 5
+PRECISIONS = {"fp32": FP32, "tf32x3": TF32X3, "bf16x3": BF16X3, "fp16x3": FP16X3, "fp64": FP64,
+              "fp64ff": FP64_FF}
 
 # Every symbol include/qflex_gb300.h declares.
 EXPORTS = (

@@ -61,6 +61,7 @@ struct Engine::Plan {
   StepDesc* d_steps = nullptr;
   float2* d_mats = nullptr;
   float2* d_mats_lo = nullptr;  // null: plain FP32 columns
+  double2* d_mats64 = nullptr;  // complex128 programs: the double gate data
   std::uint32_t* d_ptr = nullptr;
   std::uint32_t* d_leaves = nullptr;
   // Captured device pass and the buffers it was captured with.
@@ -73,6 +74,7 @@ struct Engine::Plan {
     cudaFree(d_steps);
     cudaFree(d_mats);
     cudaFree(d_mats_lo);
+    cudaFree(d_mats64);
     cudaFree(d_ptr);
     cudaFree(d_leaves);
   }
@@ -109,7 +111,7 @@ Engine::~Engine() {
 }
 
 void Engine::set_precision(int p) {
-  if (p != FP32 && p != TF32X3 && p != FP16X3 && p != BF16X3)
+  if (p != FP32 && p != TF32X3 && p != FP16X3 && p != BF16X3 && p != FP64 && p != FP64_FF)
     throw QFX_ERR("Precision mode ", p, " is not available in this build.");
   precision_ = p;
 }
@@ -197,6 +199,8 @@ void Engine::check_error_flag() {
 
 void Engine::multiply(const float2* A, const float2* B, float2* C, std::size_t m, std::size_t n,
                       std::size_t k, std::uint64_t stride, int batch) {
+  if (is_complex128(precision_))
+    throw QFX_ERR("The complex64 tensor operations need a complex64 precision mode (this context is complex128).");
   if (precision_ != FP32 && tc_eligible(m, n, k)) {
     // The tensor-core kernel reads B as [n][k]: transpose into the front of
     // the workspace, split planes after it.
@@ -283,7 +287,7 @@ namespace {
 void build_flatten_tables(const Network& net, const Program& prog, bool exact_gates,
                           std::vector<ColumnDesc>* cols, std::vector<StepDesc>* steps,
                           std::vector<float2>* mats, std::vector<float2>* mats_lo,
-                          std::uint32_t* max_log2) {
+                          std::vector<double2>* mats64, std::uint32_t* max_log2) {
   *max_log2 = 0;
   for (std::size_t c = 0; c < net.columns.size(); ++c) {
     const QubitColumn& col = net.columns[c];
@@ -307,7 +311,7 @@ void build_flatten_tables(const Network& net, const Program& prog, bool exact_ga
       StepDesc sd{};
       sd.kind = (std::uint32_t)s.kind;
       sd.V = (std::uint32_t)s.V;
-      sd.mat = (std::uint32_t)mats->size();
+      sd.mat = (std::uint32_t)(mats64 ? mats64->size() : mats->size());
       if (s.kind == 2) {
         const Link& L = net.links[s.link];
         auto it = std::find(col.indices.begin(), col.indices.end(), L.name);
@@ -320,7 +324,9 @@ void build_flatten_tables(const Network& net, const Program& prog, bool exact_ga
         }
         sd.shift = (std::uint32_t)shift;
       }
-      if (exact_gates) {
+      if (mats64) {
+        for (const auto& z : s.exact) mats64->push_back(make_double2(z.real(), z.imag()));
+      } else if (exact_gates) {
         // hi + lo of each double-precision constant
         for (const auto& z : s.exact) {
           const float hr = float(z.real()), hi = float(z.imag());
@@ -450,6 +456,34 @@ std::size_t Engine::run_program(Plan& p, int batch, float2* arena, float* tc_ws)
   return launches;
 }
 
+std::size_t Engine::run_program64(Plan& p, int batch, double2* arena) {
+  const Program& prog = p.prog;
+  std::size_t launches = 0;
+  const std::uint64_t stride = prog.arena_elems;
+  double2* scratch = reinterpret_cast<double2*>(skinny_scratch());
+  const bool ff = precision_ == FP64_FF;
+  if (profile_) {
+    while (prof_events_.size() < prog.ops.size() + 1) {
+      cudaEvent_t e;
+      QFX_CUDA(cudaEventCreate(&e));
+      prof_events_.push_back(e);
+    }
+  }
+  for (std::size_t i = 0; i < prog.ops.size(); ++i) {
+    const DevOp& op = prog.ops[i];
+    if (profile_) QFX_CUDA(cudaEventRecord(prof_events_[i], stream_));
+    if (op.kind == DevOp::PERMUTE) {
+      launch_permute64(p.perm[i], arena + op.a, arena + op.c, stride, batch, stream_);
+      launches += 1;
+    } else {
+      launch_zgemm(arena + op.a, arena + op.b, arena + op.c, op.m, op.n, op.k, stride, batch, stream_, scratch, ff);
+      launches += zskinny_splits(op.m, op.n, op.k, batch) ? 2 : 1;
+    }
+  }
+  if (profile_) QFX_CUDA(cudaEventRecord(prof_events_[prog.ops.size()], stream_));
+  return launches;
+}
+
 std::vector<OpRecord> Engine::last_ops() const {
   std::vector<OpRecord> out;
   if (!plan_ || !plan_->built) return out;
@@ -457,19 +491,23 @@ std::vector<OpRecord> Engine::last_ops() const {
   for (std::size_t i = 0; i < prog.ops.size(); ++i) {
     const DevOp& op = prog.ops[i];
     OpRecord r{};
+    const double esize = is_complex128(plan_->precision) ? 16.0 : 8.0;
     if (op.kind == DevOp::PERMUTE) {
       r.kind = 0;
       r.m = double(std::size_t(1) << op.nbits);
       r.n = r.k = 1;
-      r.bytes = 16.0 * r.m;
+      r.bytes = 2 * esize * r.m;
     } else {
       const int nb = (int)std::max<std::size_t>(stats_.batch, 1);
-      r.kind = op.b_nk ? 2 : ((vm_splits(op.m, op.n, op.k, nb) || skinny_splits(op.m, op.n, op.k, nb)) ? 3 : 1);
+      const bool split = is_complex128(plan_->precision)
+                             ? zskinny_splits(op.m, op.n, op.k, nb) != 0
+                             : (vm_splits(op.m, op.n, op.k, nb) || skinny_splits(op.m, op.n, op.k, nb));
+      r.kind = op.b_nk ? 2 : (split ? 3 : 1);
       r.m = double(op.m);
       r.n = double(op.n);
       r.k = double(op.k);
       r.flop = 8.0 * r.m * r.n * r.k;
-      r.bytes = 8.0 * (r.m * r.k + r.k * r.n + r.m * r.n);
+      r.bytes = esize * (r.m * r.k + r.k * r.n + r.m * r.n);
     }
     r.batch = double(std::max<std::size_t>(stats_.batch, 1));
     r.ms = i < op_ms_.size() ? op_ms_[i] : -1.0;
@@ -511,7 +549,7 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
   if (!p.built) {
     p.net = build_network(p.circuit, p.grid, initial, results[0].final_state, final_qubits, p.ops);
     std::function<bool(std::size_t, std::size_t, std::size_t)> b_kmajor;
-    if (precision_ != FP32) b_kmajor = tc_eligible;
+    if (precision_ != FP32 && !is_complex128(precision_)) b_kmajor = tc_eligible;
     try {
       p.prog = plan_contraction(p.net, p.ops, results[0].states.size(), INFINITY, b_kmajor, open_terminals_);
     } catch (const std::string& e) {
@@ -529,10 +567,14 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
     std::vector<ColumnDesc> cols;
     std::vector<StepDesc> steps;
     std::vector<float2> mats, mats_lo;
+    std::vector<double2> mats64;
     // The plain FP32 path keeps the reference's float gate constants; the
-    // split-precision path evaluates the columns from double constants.
+    // split-precision path evaluates the columns from double constants (in
+    // float-float), the complex128 path in FP64.
+    const bool wide = is_complex128(precision_);
     const bool exact_gates = precision_ != FP32;
-    build_flatten_tables(p.net, p.prog, exact_gates, &cols, &steps, &mats, &mats_lo, &p.max_size_log2);
+    build_flatten_tables(p.net, p.prog, exact_gates, &cols, &steps, &mats, &mats_lo, wide ? &mats64 : nullptr,
+                         &p.max_size_log2);
     std::vector<std::uint32_t> ptr(p.prog.n_amplitudes + 1, 0), leaves(p.prog.n_leaves);
     for (std::size_t l = 0; l < p.prog.n_leaves; ++l) ++ptr[p.prog.leaf_amp[l] + 1];
     for (std::size_t a = 0; a < p.prog.n_amplitudes; ++a) ptr[a + 1] += ptr[a];
@@ -541,8 +583,12 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
     if (device_ >= 0) {
       p.d_cols = upload(cols);
       p.d_steps = upload(steps);
-      p.d_mats = upload(mats);
-      if (exact_gates) p.d_mats_lo = upload(mats_lo);
+      if (wide) {
+        p.d_mats64 = upload(mats64);
+      } else {
+        p.d_mats = upload(mats);
+        if (exact_gates) p.d_mats_lo = upload(mats_lo);
+      }
       p.d_ptr = upload(ptr);
       p.d_leaves = upload(leaves);
     }
@@ -570,12 +616,13 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
   const Program& prog = p.prog;
   const std::size_t n_cols = p.net.columns.size();
   const std::size_t n_amps = prog.n_amplitudes;
-  const std::size_t arena_bytes = prog.arena_elems * sizeof(float2);
+  const bool wide = is_complex128(p.precision);
+  const std::size_t arena_bytes = prog.arena_elems * (wide ? sizeof(double2) : sizeof(float2));
   const int total = (int)finals.size();
 
   stats_ = RunStats{};
   stats_.gemm_flop = prog.gemm_flop;
-  stats_.permute_bytes = prog.permute_bytes;
+  stats_.permute_bytes = wide ? 2 * prog.permute_bytes : prog.permute_bytes;
   stats_.arena_bytes = arena_bytes;
   stats_.n_ops = prog.ops.size();
   stats_.n_leaves = prog.n_leaves;
@@ -626,6 +673,15 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
     QFX_CUDA(cudaMemsetAsync(d_amps, 0, std::max<std::size_t>(n_amps, 1) * sizeof(double2) * nb, stream_));
     QFX_CUDA(cudaEventRecord(ev0_, stream_));
     auto enqueue = [&]() -> std::size_t {
+      if (wide) {
+        double2* arena64 = reinterpret_cast<double2*>(arena);
+        launch_flatten64(p.d_cols, (int)n_cols, p.max_size_log2, p.d_steps, p.d_mats64, d_bits,
+                         d_bits + n_cols * (std::size_t)nb, arena64, prog.arena_elems, nb, stream_);
+        const std::size_t l = run_program64(p, nb, arena64) + 2;  // + flatten and sums
+        launch_reduce_amplitudes64(arena64 + prog.results_offset, prog.arena_elems, p.d_ptr, p.d_leaves,
+                                   (int)n_amps, d_amps, nb, stream_);
+        return l;
+      }
       launch_flatten(p.d_cols, (int)n_cols, p.max_size_log2, p.d_steps, p.d_mats, p.d_mats_lo, d_bits,
                      d_bits + n_cols * (std::size_t)nb, arena, prog.arena_elems, nb, stream_);
       const std::size_t l = run_program(p, nb, arena, tc_ws) + 2;  // + flatten and sums

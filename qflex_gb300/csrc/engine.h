@@ -17,7 +17,10 @@
 
 namespace qfx {
 
-enum Precision : int { FP32 = 0, TF32X3 = 1, BF16X3 = 2, FP16X3 = 3 };
+// FP64 and FP64_FF run the contraction in complex128 (the GPU oracle):
+// FP64 with FP64 FMAs throughout, FP64_FF with float-float tiled products.
+enum Precision : int { FP32 = 0, TF32X3 = 1, BF16X3 = 2, FP16X3 = 3, FP64 = 4, FP64_FF = 5 };
+inline bool is_complex128(int precision) { return precision == FP64 || precision == FP64_FF; }
 
 struct EvalResult {
   std::string initial_state;  // as mutated by EvaluateCircuit
@@ -104,6 +107,8 @@ class Engine {
   struct Plan;
   Plan* get_plan(const std::string& circuit, const std::string& ordering, const std::string& grid);
   std::size_t run_program(Plan& p, int batch, float2* arena, float* tc_ws);
+  // The same program in complex128 (FP64 and FP64_FF).
+  std::size_t run_program64(Plan& p, int batch, double2* arena);
   // Marks permute/product pairs whose A operand goes straight into planes.
   void plan_fusion(Plan& p);
 

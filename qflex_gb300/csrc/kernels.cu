@@ -138,21 +138,22 @@ struct PlaneOut {
   std::uint32_t k_log2;
 };
 
-template <bool PLANES>
+// E is the element: float2 (complex64) or double2 (complex128; no planes).
+template <typename E, bool PLANES>
 __global__ void __launch_bounds__(256, 8) permute_kernel(const __grid_constant__ PermPlan P,
-                                                      const float2* __restrict__ src,
-                                                      float2* __restrict__ dst,
+                                                      const E* __restrict__ src,
+                                                      E* __restrict__ dst,
                                                       std::uint64_t batch_stride, PlaneOut po) {
-  __shared__ float2 tile[1024];
+  __shared__ E tile[1024];
   __shared__ std::uint32_t tab[6 * 32];
   if (threadIdx.x < 6 * 32) tab[threadIdx.x] = P.tab[threadIdx.x / 32][threadIdx.x % 32];
   __syncthreads();
   const std::uint32_t T = 1u << P.tile_bits;
-  const float2* s = src + std::uint64_t(blockIdx.y) * batch_stride;
-  float2* d = dst + std::uint64_t(blockIdx.y) * batch_stride;
+  const E* s = src + std::uint64_t(blockIdx.y) * batch_stride;
+  E* d = dst + std::uint64_t(blockIdx.y) * batch_stride;
   // The next tile's loads are issued into registers before the current
   // tile is stored, so loads stay in flight through the store phase.
-  float2 r[4];
+  E r[4];
   auto load = [&](std::uint64_t t) {
     std::uint64_t bi, bo;
     perm_tile_base(P, t, &bi, &bo);
@@ -179,11 +180,11 @@ __global__ void __launch_bounds__(256, 8) permute_kernel(const __grid_constant__
       const std::uint32_t j = threadIdx.x + 256u * i;
       if (j >= T) continue;  // T is a multiple of 32 here: whole warps
       const std::uint64_t o = bo + tab[64 + (j & 31)] + tab[96 + (j >> 5)];
-      const float2 v = tile[perm_swizzle(tab[128 + (j & 31)] + tab[160 + (j >> 5)])];
-      if (!PLANES) {
+      const E v = tile[perm_swizzle(tab[128 + (j & 31)] + tab[160 + (j >> 5)])];
+      if constexpr (!PLANES) {
         d[o] = v;
         continue;
-      }
+      } else {
       // The warp's 32 values are outputs o - lane .. o - lane + 31: one
       // 32-aligned run of a row (the tile holds the 5 lowest output digits).
       // Its largest |re| or |im|: bit patterns of non-negative floats order
@@ -218,6 +219,7 @@ __global__ void __launch_bounds__(256, 8) permute_kernel(const __grid_constant__
       pl[48] = __high2half(lo);
       if ((threadIdx.x & 31) == 0)
         po.exps[std::uint64_t(blockIdx.y) * po.rows * (k / 32) + row * (k / 32) + kk / 32] = e;
+      }
     }
     __syncthreads();
   }
@@ -639,8 +641,17 @@ void launch_permute(const PermPlan& plan, const float2* src, float2* dst, std::u
   const std::uint64_t tiles = plan.n_tiles;
   const unsigned gx = (unsigned)std::min<std::uint64_t>(tiles, 152ull * 16ull);
   dim3 grid(gx, (unsigned)batch, 1);
-  permute_kernel<false><<<grid, 256, 0, s>>>(plan, src, dst, batch_stride, PlaneOut{});
+  permute_kernel<float2, false><<<grid, 256, 0, s>>>(plan, src, dst, batch_stride, PlaneOut{});
   check_launch("permute");
+}
+
+void launch_permute64(const PermPlan& plan, const double2* src, double2* dst, std::uint64_t batch_stride,
+                      int batch, cudaStream_t s) {
+  const std::uint64_t tiles = plan.n_tiles;
+  const unsigned gx = (unsigned)std::min<std::uint64_t>(tiles, 152ull * 8ull);
+  dim3 grid(gx, (unsigned)batch, 1);
+  permute_kernel<double2, false><<<grid, 256, 0, s>>>(plan, src, dst, batch_stride, PlaneOut{});
+  check_launch("permute64");
 }
 
 void launch_permute_fp16_planes(const PermPlan& plan, const float2* src, std::uint64_t src_batch_stride,
@@ -651,7 +662,7 @@ void launch_permute_fp16_planes(const PermPlan& plan, const float2* src, std::ui
   const std::uint64_t tiles = plan.n_tiles;
   const unsigned gx = (unsigned)std::min<std::uint64_t>(tiles, 152ull * 16ull);
   dim3 grid(gx, (unsigned)batch, 1);
-  permute_kernel<true><<<grid, 256, 0, s>>>(plan, src, nullptr, src_batch_stride,
+  permute_kernel<float2, true><<<grid, 256, 0, s>>>(plan, src, nullptr, src_batch_stride,
                                             PlaneOut{static_cast<__half*>(planes), exps, rows, (std::uint32_t)k_log2});
   check_launch("permute_fp16_planes");
 }

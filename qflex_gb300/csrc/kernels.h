@@ -110,6 +110,27 @@ void launch_cgemm_fp32(const float2* A, const float2* B, float2* C, std::size_t 
 void launch_skinny_split(const float2* A, const float2* B, float2* C, std::size_t m, std::size_t n,
                         std::size_t k, int splits, float2* partial, cudaStream_t s);
 
+// ---- complex128 path (the FP64 GPU oracle, kernels64.cu) ----------------------
+// Same layouts and index schedules as the complex64 kernels, with double2
+// elements. Gate data are the double-precision gate constants.
+void launch_flatten64(const ColumnDesc* cols, int n_cols, std::uint32_t max_size_log2, const StepDesc* steps,
+                      const double2* mats, const std::uint8_t* init_bits, const std::uint8_t* final_bits,
+                      double2* arena, std::uint64_t arena_stride, int batch, cudaStream_t s);
+void launch_permute64(const PermPlan& plan, const double2* src, double2* dst, std::uint64_t batch_stride,
+                      int batch, cudaStream_t s);
+// Split-k partial sums of the complex128 skinny products share the skinny
+// scratch buffer (kSkinnyScratchElems float2 = this many double2).
+constexpr std::size_t kSkinnyScratchElems64 = kSkinnyScratchElems / 2;
+int zskinny_splits(std::size_t m, std::size_t n, std::size_t k, int batch);
+// C[m,n] = A[m,k] * B[k,n] in complex128. `ff` selects float-float
+// arithmetic for the tiled products (FP64 FMA otherwise); skinny products
+// and GEMVs always use FP64 FMA.
+void launch_zgemm(const double2* A, const double2* B, double2* C, std::size_t m, std::size_t n, std::size_t k,
+                  std::uint64_t batch_stride, int batch, cudaStream_t s, double2* scratch, bool ff);
+void launch_reduce_amplitudes64(const double2* results, std::uint64_t stride, const std::uint32_t* ptr,
+                                const std::uint32_t* leaves, int n_amps, double2* amps, int batch,
+                                cudaStream_t s);
+
 // ---- FP64 amplitude sums -------------------------------------------------------
 // amps[b * n_amps + a] += sum of results[b * stride + leaf] over the leaves
 // of amplitude a (CSR: leaves[ptr[a] .. ptr[a+1])), in leaf order.

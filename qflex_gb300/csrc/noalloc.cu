@@ -51,14 +51,15 @@ extern "C" int qflex_gb300_multiply_skinny_noalloc(const void* A, const void* B,
     put_error(err, err_len, "A, B and C must be non-null device pointers.");
     return QFLEX_GB300_ERR_ARG;
   }
-  const std::size_t outputs = m * n;
-  if (outputs == 0) return QFLEX_GB300_OK;
-  if (m > 64 || n > 64 || outputs > 64) {
+  // m and n are bounded before m * n is formed, so the product cannot wrap.
+  if (m > 64 || n > 64 || m * n > 64) {
     put_error(err, err_len,
               "qflex_gb300_multiply_skinny_noalloc takes at most 64 outputs (m * n <= 64); use "
               "qflex_gb300_multiply for larger products.");
     return QFLEX_GB300_ERR_ARG;
   }
+  const std::size_t outputs = m * n;
+  if (outputs == 0) return QFLEX_GB300_OK;
   // One split per 4096 terms, capped so outputs * splits fits the array.
   std::size_t splits = (k + 4095) / 4096;
   if (splits < 1) splits = 1;

@@ -178,6 +178,15 @@ def workload(name: str, seed: int = 0):
     return circuit, ordering, grid_text(I, J), initial, finals
 
 
+# Real flop (8 m n k summed over the complex products) of one amplitude of
+# the c3 workload, keyed by the number of cut slices summed: 16 for the
+# workload's ordering, 4 for ordering_7x7((0,), (0, 1, 2, 3)) and 1 for
+# ordering_7x7((0,), (0,)). They depend on the ordering only, not on the
+# strings. The CPU baseline scales a timed sample of slices to the 16-slice
+# amplitude with them.
+C3_GEMM_FLOP = {16: 14910827790336.0, 4: 3964990390272.0, 1: 1772918145024.0}
+
+
 def ordering_6x6(cut_values: Optional[Sequence[int]] = None) -> str:
     """6x6: cut the vertical bond (2,3)-(3,3) first, contract the top half
     (rows 0-2) and the bottom half (rows 5..3) as two patches, row by row
