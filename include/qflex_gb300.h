@@ -139,6 +139,13 @@ size_t qflex_gb300_last_ops(const qflex_gb300_context* ctx, double* out, size_t 
  *                planes (scaled per 32 values of a row) directly instead of
  *                complex64, and the product skips splitting A (default 1,
  *                or QFLEX_GB300_FUSE)
+ *   "tc_wait_ns" limit in ns of every pipeline wait of the tensor-core
+ *                products (0: 2 s, the default). A wait that runs out stops its
+ *                thread block, which drains the copies and MMAs it started,
+ *                frees its tensor memory and returns; the call (or the next
+ *                qflex_gb300_synchronize after qflex_gb300_multiply) returns
+ *                QFLEX_GB300_ERR_CUDA, "tensor-core pipeline wait expired", and
+ *                the context stays usable. For tests of that path.
  *   "open_terminals" 1: terminal cuts that take all their values, with no
  *                two-qubit cut after them, stay open indices -- the ops after
  *                them run once on tensors carrying the open indices instead
@@ -160,17 +167,21 @@ int qflex_gb300_set_tc_variant(qflex_gb300_context* ctx, size_t m, size_t n, siz
 
 /* Out-of-place index permutation: the data movement of Tensor::reorder
  * (src/tensor.cpp:866-911). The tensor has `rank` indices with dimensions
- * `dims` (row-major, last index fastest, every dimension a power of two);
- * `new_order[i]` is the old position of the index that goes to position i.
- * `batch` tensors at a distance of `batch_stride` elements are permuted. */
+ * `dims` (row-major, last index fastest); `new_order[i]` is the old position
+ * of the index that goes to position i. `batch` tensors at a distance of
+ * `batch_stride` elements are permuted. When every dimension is a power of
+ * two (the only dimensions a contraction creates) the tiled binary-digit
+ * kernel runs (the reference's _fast_reorder, src/tensor.cpp:494-864);
+ * otherwise a general gather kernel (its _naive_reorder,
+ * src/tensor.cpp:377-492), for at most 32 indices. */
 int qflex_gb300_permute(qflex_gb300_context* ctx, const void* src, void* dst, size_t rank,
                         const size_t* dims, const size_t* new_order, size_t batch,
                         size_t batch_stride);
 
-/* Host-side check of the permutation kernel's tiling: runs the kernel's
- * exact index schedule (same tables, same tile order) over HOST buffers of
- * complex64. For tests and diagnostics; needs no GPU and no context. No
- * reference counterpart. */
+/* Host-side check of the permutation kernels' index math: runs the chosen
+ * kernel's exact schedule (same tables, same tile order, or the general
+ * kernel's index decomposition) over HOST buffers of complex64. For tests
+ * and diagnostics; needs no GPU and no context. No reference counterpart. */
 int qflex_gb300_check_permute(size_t rank, const size_t* dims, const size_t* new_order,
                               const void* src_host, void* dst_host);
 
@@ -188,6 +199,40 @@ int qflex_gb300_multiply(qflex_gb300_context* ctx, const void* A, const void* B,
                          size_t n, size_t k, size_t batch, size_t batch_stride);
 
 int qflex_gb300_synchronize(qflex_gb300_context* ctx);
+
+/* ---- the input models, parsed ----
+ * The reference's QflexCircuit / QflexGrid / QflexOrdering parse their text
+ * in load() and expose the parsed members (src/circuit.h, src/grid.h,
+ * src/ordering.h); these functions run the parsers EvaluateCircuit uses and
+ * return the same members. Errors return QFLEX_GB300_ERR_INPUT with the
+ * reference's message in `err` (`err_len` bytes, may be NULL). */
+typedef struct qflex_gb300_circuit qflex_gb300_circuit;
+/* QflexCircuit::load (src/circuit.cpp:30-206). Free with
+ * qflex_gb300_circuit_free. */
+int qflex_gb300_circuit_load(const char* text, qflex_gb300_circuit** out, char* err, size_t err_len);
+void qflex_gb300_circuit_free(qflex_gb300_circuit* circuit);
+/* QflexCircuit::num_active_qubits, depth and gates.size(). */
+size_t qflex_gb300_circuit_num_active_qubits(const qflex_gb300_circuit* circuit);
+size_t qflex_gb300_circuit_depth(const qflex_gb300_circuit* circuit);
+size_t qflex_gb300_circuit_gate_count(const qflex_gb300_circuit* circuit);
+/* Gate `i` (QflexGate, src/circuit.h): `name` and `raw` (the cleaned line)
+ * stay owned by `circuit`; up to `qubits_cap` qubits and `params_cap`
+ * parameters are written, and their full counts go to *n_qubits and
+ * *n_params. */
+int qflex_gb300_circuit_gate(const qflex_gb300_circuit* circuit, size_t i, const char** name, const char** raw,
+                             size_t* cycle, size_t* qubits, size_t qubits_cap, size_t* n_qubits, double* params,
+                             size_t params_cap, size_t* n_params);
+/* QflexGrid::load (src/grid.cpp:11-45): I, J and the off qubits as
+ * (row, column) pairs, up to `off_cap` pairs into `off`; *n_off gets the
+ * full count. */
+int qflex_gb300_grid_load(const char* text, size_t* I, size_t* J, size_t* off, size_t off_cap, size_t* n_off,
+                          char* err, size_t err_len);
+/* QflexOrdering::load (src/ordering.cpp:10-45): the cleaned instruction
+ * lines joined by '\n' into `out` (NUL-terminated, at most `cap` bytes);
+ * *needed gets the bytes required including the NUL, *n_instructions the
+ * number of lines. */
+int qflex_gb300_ordering_load(const char* text, char* out, size_t cap, size_t* n_instructions, size_t* needed,
+                              char* err, size_t err_len);
 
 /* ---- learned cost model kernels ----
  * A 3-layer perceptron y = W3 relu(W2 relu(W1 x + b1) + b2) + b3 in FP32

@@ -12,6 +12,9 @@
 //   qflex_ref reorder <n_binary> <perm...>
 //       tensor of n binary indices named i0..i(n-1) with data[p] = p,
 //       reordered to (i<perm[0]>, ...); prints the real parts.
+//   qflex_ref reorder_dims <n> <dim...> <perm...>
+//       the same with n indices of the given dimensions (any sizes; the
+//       reference reorders those with its naive path).
 //   qflex_ref threads <n> eval ...   (sets the OpenBLAS thread count first)
 //   qflex_ref [threads <n>] time <reps> eval ...
 //       runs EvaluateCircuit <reps> times on the loaded input and prints
@@ -95,6 +98,30 @@ static int do_reorder(int argc, char** argv) {
   return 0;
 }
 
+static int do_reorder_dims(int argc, char** argv) {
+  const std::size_t n = std::strtoul(argv[2], nullptr, 10);
+  if (argc < int(3 + 2 * n)) {
+    std::fprintf(stderr, "reorder_dims needs n dimensions and n positions\n");
+    return 64;
+  }
+  std::vector<std::string> names(n), order;
+  std::vector<std::size_t> dims(n);
+  std::size_t size = 1;
+  for (std::size_t i = 0; i < n; ++i) {
+    names[i] = "i" + std::to_string(i);
+    dims[i] = std::strtoul(argv[3 + i], nullptr, 10);
+    size *= dims[i];
+  }
+  for (std::size_t i = 0; i < n; ++i) order.push_back(names[std::atoi(argv[3 + n + i])]);
+  std::vector<qflex::s_type> data(size);
+  for (std::size_t p = 0; p < size; ++p) data[p] = qflex::s_type(float(p), 0.f);
+  qflex::Tensor t(names, dims, data);
+  std::vector<qflex::s_type> scratch(size);
+  t.reorder(order, scratch.data());
+  for (std::size_t p = 0; p < size; ++p) std::printf("%ld\n", (long)t.data()[p].real());
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc >= 3 && !std::strcmp(argv[1], "threads")) {
     scipy_openblas_set_num_threads(std::atoi(argv[2]));
@@ -112,6 +139,7 @@ int main(int argc, char** argv) {
   if (argc >= 2 && !std::strcmp(argv[1], "eval")) return do_eval(argc, argv, reps);
   if (argc >= 3 && !std::strcmp(argv[1], "reorder"))
     return do_reorder(argc, argv);
+  if (argc >= 3 && !std::strcmp(argv[1], "reorder_dims")) return do_reorder_dims(argc, argv);
   std::fprintf(stderr, "usage: qflex_ref [threads N] eval|reorder ...\n");
   return 64;
 }

@@ -31,6 +31,9 @@ EXPORTS = (
     "qflex_gb300_multiply", "qflex_gb300_synchronize", "qflex_gb300_mlp_param_count",
     "qflex_gb300_mlp_work_floats", "qflex_gb300_mlp_forward", "qflex_gb300_mlp_loss_grad",
     "qflex_gb300_mlp_adam", "qflex_gb300_multiply_skinny_noalloc",
+    "qflex_gb300_circuit_load", "qflex_gb300_circuit_free", "qflex_gb300_circuit_num_active_qubits",
+    "qflex_gb300_circuit_depth", "qflex_gb300_circuit_gate_count", "qflex_gb300_circuit_gate",
+    "qflex_gb300_grid_load", "qflex_gb300_ordering_load",
 )
 
 
@@ -107,6 +110,16 @@ def load_library(path: Optional[Path] = None) -> C.CDLL:
             "qflex_gb300_mlp_forward": (i, [vp, vp, vp, sz, i, i, vp, vp]),
             "qflex_gb300_mlp_loss_grad": (i, [vp, vp, vp, vp, sz, i, i, vp, vp, vp]),
             "qflex_gb300_mlp_adam": (i, [vp, vp, vp, vp, vp, sz, i, C.c_float]),
+            "qflex_gb300_circuit_load": (i, [cp, C.POINTER(vp), cp, sz]),
+            "qflex_gb300_circuit_free": (None, [vp]),
+            "qflex_gb300_circuit_num_active_qubits": (sz, [vp]),
+            "qflex_gb300_circuit_depth": (sz, [vp]),
+            "qflex_gb300_circuit_gate_count": (sz, [vp]),
+            "qflex_gb300_circuit_gate": (i, [vp, sz, C.POINTER(cp), C.POINTER(cp), C.POINTER(sz), C.POINTER(sz), sz,
+                                             C.POINTER(sz), C.POINTER(dbl), sz, C.POINTER(sz)]),
+            "qflex_gb300_grid_load": (i, [cp, C.POINTER(sz), C.POINTER(sz), C.POINTER(sz), sz, C.POINTER(sz), cp,
+                                          sz]),
+            "qflex_gb300_ordering_load": (i, [cp, cp, sz, C.POINTER(sz), C.POINTER(sz), cp, sz]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)

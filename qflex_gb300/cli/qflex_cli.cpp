@@ -4,7 +4,7 @@
 //
 //   qflex <circuit> <ordering> <grid> [<initial_conf> <final_conf> <verbosity> <memory_limit>]
 //   qflex -c <circuit> -o <ordering> -g <grid> [--initial-conf=S] [--final-conf=S]
-//         [--verbosity=N] [--memory=M] [--device=N] [--precision=fp32|tf32x3|fp16x3|bf16x3]
+//         [--verbosity=N] [--memory=M] [--device=N] [--precision=fp32|tf32x3|fp16x3|bf16x3|fp64|fp64ff]
 //
 // Output: one line "<initial> --> <state>: <re> <im>" per amplitude.
 // Exit codes: 0 ok, 1 std::exception, 2 error message (thrown string).
@@ -42,7 +42,7 @@ const char* kUsage =
     "  qflex <circuit_filename> <ordering_filename> <grid_filename> [<initial_conf> <final_conf> "
     "<verbosity_level> <memory_limit>]\n"
     "  qflex -c <circuit_filename> -o <ordering_filename> -g <grid_filename> [--initial-conf=S "
-    "--final-conf=S --verbosity=N --memory=M --device=N --precision=fp32|tf32x3|fp16x3|bf16x3]\n";
+    "--final-conf=S --verbosity=N --memory=M --device=N --precision=fp32|tf32x3|fp16x3|bf16x3|fp64|fp64ff]\n";
 
 }  // namespace
 
@@ -93,13 +93,22 @@ int main(int argc, char** argv) {
         qflex::global::precision = QFLEX_GB300_FP16X3;
       else if (p == "bf16x3")
         qflex::global::precision = QFLEX_GB300_BF16X3;
+      else if (p == "fp64")
+        qflex::global::precision = QFLEX_GB300_FP64;
+      else if (p == "fp64ff")
+        qflex::global::precision = QFLEX_GB300_FP64_FF;
       else
         throw std::string("Unknown precision ") + p;
     }
     input.circuit.load(circuit);
     input.ordering.load(ordering);
     input.grid.load(grid);
-    auto amplitudes = qflex::EvaluateCircuit(&input);
+    std::vector<std::pair<std::string, std::complex<double>>> amplitudes;
+    try {
+      amplitudes = qflex::EvaluateCircuit(&input);
+    } catch (const std::string& msg) {
+      throw std::string("ERROR (qflex_gb300: main) --> Failed to call EvaluateCircuit(). Error:\n\t[") + msg + "]";
+    }
     std::cout.precision(17);
     for (const auto& [state, amp] : amplitudes)
       std::cout << input.initial_state << " --> " << state << ": " << amp.real() << " " << amp.imag() << "\n";

@@ -1,5 +1,6 @@
 // extern "C" boundary of the engine (declared in include/qflex_gb300.h).
 // Converts thrown std::string / std::exception into status codes.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <exception>
@@ -56,6 +57,55 @@ void store(qflex_gb300_context* ctx, std::vector<qfx::EvalResult>&& res) {
       ctx->amps.push_back(r.amplitudes[i]);
     }
   }
+}
+
+bool all_powers_of_two(std::size_t rank, const std::size_t* dims) {
+  for (std::size_t i = 0; i < rank; ++i)
+    if (dims[i] == 0 || (dims[i] & (dims[i] - 1)) != 0) return false;
+  return true;
+}
+
+// A permutation of any dimensions: the binary-digit plan when every
+// dimension is a power of two, the general gather otherwise.
+struct AnyPerm {
+  bool binary = true;
+  int nbits = 0;
+  qfx::PermPlan plan;
+  qfx::GeneralPerm general;
+  std::uint64_t size() const { return binary ? (std::uint64_t(1) << nbits) : general.size; }
+};
+
+void check_perm(std::size_t rank, const std::size_t* dims, const std::size_t* order, int* nbits,
+                std::uint8_t* perm);
+
+void plan_any_perm(std::size_t rank, const std::size_t* dims, const std::size_t* order, AnyPerm* out,
+                   bool* identity = nullptr) {
+  if (rank > 0 && (!dims || !order)) throw QFX_ERR("dims and new_order must be non-null.");
+  if (all_powers_of_two(rank, dims)) {
+    std::uint8_t perm[40] = {};
+    check_perm(rank, dims, order, &out->nbits, perm);
+    out->binary = true;
+    qfx::make_perm_plan(out->nbits, perm, &out->plan);
+    if (identity) {
+      *identity = true;
+      for (int b = 0; b < out->nbits; ++b) *identity &= perm[b] == b;
+    }
+  } else {
+    out->binary = false;
+    qfx::make_general_perm(rank, dims, order, &out->general);
+    if (identity) {
+      *identity = true;
+      for (std::size_t i = 0; i < rank; ++i) *identity &= order[i] == i;
+    }
+  }
+}
+
+void launch_any_perm(const AnyPerm& p, const float2* src, float2* dst, std::uint64_t batch_stride, int batch,
+                     cudaStream_t s) {
+  if (p.binary)
+    qfx::launch_permute(p.plan, src, dst, batch_stride, batch, s);
+  else
+    qfx::launch_permute_general(p.general, src, dst, batch_stride, batch, s);
 }
 
 void check_perm(std::size_t rank, const std::size_t* dims, const std::size_t* order, int* nbits,
@@ -266,14 +316,12 @@ int qflex_gb300_permute(qflex_gb300_context* ctx, const void* src, void* dst, si
     if (src == dst) throw QFX_ERR("src and dst must not overlap; use qflex_gb300_reorder.");
     if (batch == 0) return;
     if (batch > 65535) throw QFX_ERR("batch must be at most 65535.");
-    int nbits = 0;
-    std::uint8_t perm[40] = {};
-    check_perm(rank, dims, new_order, &nbits, perm);
-    qfx::PermPlan plan;
-    qfx::make_perm_plan(nbits, perm, &plan);
+    if (qfx::is_complex128(ctx->engine->precision()))
+      throw QFX_ERR("The complex64 tensor operations need a complex64 precision mode (this context is complex128).");
+    AnyPerm p;
+    plan_any_perm(rank, dims, new_order, &p);
     cudaSetDevice(ctx->engine->device());
-    qfx::launch_permute(plan, (const float2*)src, (float2*)dst, batch_stride, (int)batch,
-                        ctx->engine->stream());
+    launch_any_perm(p, (const float2*)src, (float2*)dst, batch_stride, (int)batch, ctx->engine->stream());
   });
 }
 
@@ -281,13 +329,12 @@ int qflex_gb300_check_permute(size_t rank, const size_t* dims, const size_t* new
                               const void* src_host, void* dst_host) {
   try {
     if (!src_host || !dst_host) return QFLEX_GB300_ERR_ARG;
-    int nbits = 0;
-    std::uint8_t perm[40] = {};
-    check_perm(rank, dims, new_order, &nbits, perm);
-    qfx::PermPlan plan;
-    qfx::make_perm_plan(nbits, perm, &plan);
-    qfx::permute_schedule_on_host(plan, (const float2*)src_host, (float2*)dst_host,
-                                  std::uint64_t(1) << nbits);
+    AnyPerm p;
+    plan_any_perm(rank, dims, new_order, &p);
+    if (p.binary)
+      qfx::permute_schedule_on_host(p.plan, (const float2*)src_host, (float2*)dst_host, p.size());
+    else
+      qfx::permute_general_on_host(p.general, (const float2*)src_host, (float2*)dst_host);
     return QFLEX_GB300_OK;
   } catch (...) {
     return QFLEX_GB300_ERR_ARG;
@@ -300,18 +347,16 @@ int qflex_gb300_reorder(qflex_gb300_context* ctx, void* data, void* scratch, siz
     if (!ctx->engine) throw QFX_ERR("context has no engine");
     if (!scratch) throw QFX_ERR("Scratch copy must be non-null.");
     if (!data) throw QFX_ERR("Data must be non-null.");
-    int nbits = 0;
-    std::uint8_t perm[40] = {};
-    check_perm(rank, dims, new_order, &nbits, perm);
-    bool identity = true;
-    for (int b = 0; b < nbits; ++b) identity &= perm[b] == b;
+    if (qfx::is_complex128(ctx->engine->precision()))
+      throw QFX_ERR("The complex64 tensor operations need a complex64 precision mode (this context is complex128).");
+    AnyPerm p;
+    bool identity = false;
+    plan_any_perm(rank, dims, new_order, &p, &identity);
     if (identity) return;
-    qfx::PermPlan plan;
-    qfx::make_perm_plan(nbits, perm, &plan);
     cudaSetDevice(ctx->engine->device());
-    qfx::launch_permute(plan, (const float2*)data, (float2*)scratch, 0, 1, ctx->engine->stream());
-    cudaError_t e = cudaMemcpyAsync(data, scratch, (std::size_t(1) << nbits) * sizeof(float2),
-                                    cudaMemcpyDeviceToDevice, ctx->engine->stream());
+    launch_any_perm(p, (const float2*)data, (float2*)scratch, 0, 1, ctx->engine->stream());
+    cudaError_t e = cudaMemcpyAsync(data, scratch, p.size() * sizeof(float2), cudaMemcpyDeviceToDevice,
+                                    ctx->engine->stream());
     if (e != cudaSuccess) throw qfx::cuda_error_string(e, "cudaMemcpyAsync");
   });
 }
@@ -333,11 +378,121 @@ int qflex_gb300_multiply(qflex_gb300_context* ctx, const void* A, const void* B,
   });
 }
 
+}  // extern "C"
+
+struct qflex_gb300_circuit {
+  qfx::Circuit circuit;
+};
+
+namespace {
+
+// Runs a parser; reference errors become QFLEX_GB300_ERR_INPUT with the
+// message in `err`.
+template <typename F>
+int parse_guarded(char* err, std::size_t err_len, F&& f) {
+  auto put = [&](const std::string& msg) {
+    if (err && err_len) {
+      std::strncpy(err, msg.c_str(), err_len - 1);
+      err[err_len - 1] = '\0';
+    }
+  };
+  try {
+    f();
+    put("");
+    return QFLEX_GB300_OK;
+  } catch (const std::string& e) {
+    put(e);
+    return QFLEX_GB300_ERR_INPUT;
+  } catch (const std::bad_alloc&) {
+    put("ERROR (qflex_gb300) --> host allocation failed");
+    return QFLEX_GB300_ERR_ARG;
+  } catch (const std::exception& e) {
+    put(e.what());
+    return QFLEX_GB300_ERR_INPUT;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int qflex_gb300_circuit_load(const char* text, qflex_gb300_circuit** out, char* err, size_t err_len) {
+  if (!out) return QFLEX_GB300_ERR_ARG;
+  *out = nullptr;
+  auto c = std::make_unique<qflex_gb300_circuit>();
+  const int rc = parse_guarded(err, err_len, [&] { c->circuit.load(text ? text : ""); });
+  if (rc == QFLEX_GB300_OK) *out = c.release();
+  return rc;
+}
+
+void qflex_gb300_circuit_free(qflex_gb300_circuit* circuit) { delete circuit; }
+
+size_t qflex_gb300_circuit_num_active_qubits(const qflex_gb300_circuit* c) {
+  return c ? (size_t)c->circuit.num_active_qubits : 0;
+}
+
+size_t qflex_gb300_circuit_depth(const qflex_gb300_circuit* c) { return c ? (size_t)c->circuit.depth : 0; }
+
+size_t qflex_gb300_circuit_gate_count(const qflex_gb300_circuit* c) { return c ? c->circuit.gates.size() : 0; }
+
+int qflex_gb300_circuit_gate(const qflex_gb300_circuit* c, size_t i, const char** name, const char** raw,
+                             size_t* cycle, size_t* qubits, size_t qubits_cap, size_t* n_qubits, double* params,
+                             size_t params_cap, size_t* n_params) {
+  if (!c || i >= c->circuit.gates.size()) return QFLEX_GB300_ERR_ARG;
+  const qfx::Gate& g = c->circuit.gates[i];
+  if (name) *name = g.name.c_str();
+  if (raw) *raw = g.raw.c_str();
+  if (cycle) *cycle = (size_t)g.cycle;
+  for (size_t q = 0; q < g.qubits.size() && q < qubits_cap && qubits; ++q) qubits[q] = (size_t)g.qubits[q];
+  if (n_qubits) *n_qubits = g.qubits.size();
+  for (size_t q = 0; q < g.params.size() && q < params_cap && params; ++q) params[q] = g.params[q];
+  if (n_params) *n_params = g.params.size();
+  return QFLEX_GB300_OK;
+}
+
+int qflex_gb300_grid_load(const char* text, size_t* I, size_t* J, size_t* off, size_t off_cap, size_t* n_off,
+                          char* err, size_t err_len) {
+  return parse_guarded(err, err_len, [&] {
+    qfx::Grid g;
+    g.load(text ? text : "");
+    if (I) *I = (size_t)g.I;
+    if (J) *J = (size_t)g.J;
+    for (size_t q = 0; q < g.qubits_off.size() && q < off_cap && off; ++q) {
+      off[2 * q] = (size_t)g.qubits_off[q].first;
+      off[2 * q + 1] = (size_t)g.qubits_off[q].second;
+    }
+    if (n_off) *n_off = g.qubits_off.size();
+  });
+}
+
+int qflex_gb300_ordering_load(const char* text, char* out, size_t cap, size_t* n_instructions, size_t* needed,
+                              char* err, size_t err_len) {
+  return parse_guarded(err, err_len, [&] {
+    qfx::Ordering o;
+    o.load(text ? text : "");
+    std::string joined;
+    for (size_t i = 0; i < o.instructions.size(); ++i) {
+      if (i) joined += '\n';
+      joined += o.instructions[i];
+    }
+    if (n_instructions) *n_instructions = o.instructions.size();
+    if (needed) *needed = joined.size() + 1;
+    if (out && cap) {
+      const size_t n = std::min(cap - 1, joined.size());
+      std::memcpy(out, joined.data(), n);
+      out[n] = '\0';
+    }
+  });
+}
+
 int qflex_gb300_synchronize(qflex_gb300_context* ctx) {
   return guarded(ctx, [&] {
     if (!ctx->engine) throw QFX_ERR("context has no engine");
     cudaError_t e = cudaStreamSynchronize(ctx->engine->stream());
     if (e != cudaSuccess) throw qfx::cuda_error_string(e, "cudaStreamSynchronize");
+    // A tensor-core product queued by qflex_gb300_multiply reports an
+    // expired pipeline wait here.
+    if (ctx->engine->has_error_flag()) ctx->engine->check_error_flag();
   });
 }
 

@@ -133,6 +133,15 @@ void Engine::set_option(const std::string& name, double value) {
   } else if (name == "open_terminals") {
     if (value != 0 && value != 1) throw QFX_ERR("Option open_terminals must be 0 or 1.");
     open_terminals_ = value != 0;
+  } else if (name == "tc_wait_ns") {
+    if (!(value >= 0 && value <= 1e11) || value != double((unsigned long long)value))
+      throw QFX_ERR("Option tc_wait_ns must be an integer in 0..1e11.");
+    wait_ns_ = (unsigned long long)value;
+    if (device_ >= 0) {
+      int* p = error_flag();
+      QFX_CUDA(cudaMemcpyAsync(p + 2, &wait_ns_, sizeof(wait_ns_), cudaMemcpyHostToDevice, stream_));
+      QFX_CUDA(cudaStreamSynchronize(stream_));
+    }
   } else if (name == "max_batch") {
     if (!(value >= 0 && value <= 65535) || value != double(int(value)))
       throw QFX_ERR("Option max_batch must be an integer in 0..65535.");
@@ -150,6 +159,7 @@ double Engine::get_option(const std::string& name) const {
   if (name == "max_batch") return max_batch_;
   if (name == "open_terminals") return open_terminals_ ? 1 : 0;
   if (name == "fuse_splits") return fuse_splits_ ? 1 : 0;
+  if (name == "tc_wait_ns") return double(wait_ns_);
   throw QFX_ERR("Unknown option '", name, "'.");
 }
 
@@ -181,7 +191,18 @@ TcConfig Engine::tc_config(std::size_t m, std::size_t n, std::size_t k) const {
   return c;
 }
 
-int* Engine::error_flag() { return (int*)reserve(sizeof(int) * 4, 5); }
+int* Engine::error_flag() {
+  // int[4]: the error code of the tensor-core kernels, then (bytes 8..15)
+  // the limit of their pipeline waits in ns (0: the kernels' 2 s default).
+  const bool fresh = (int)bufs_.size() <= 5 || bufs_[5].bytes < 4 * sizeof(int);
+  int* p = (int*)reserve(sizeof(int) * 4, 5);
+  if (fresh) {
+    const unsigned long long init[2] = {0ull, wait_ns_};
+    QFX_CUDA(cudaMemcpyAsync(p, init, sizeof(init), cudaMemcpyHostToDevice, stream_));
+    QFX_CUDA(cudaStreamSynchronize(stream_));
+  }
+  return p;
+}
 
 float* Engine::tc_workspace(std::size_t elems) {
   return (float*)reserve(std::max<std::size_t>(elems, 1) * sizeof(float), 4);
@@ -193,7 +214,8 @@ void Engine::check_error_flag() {
   QFX_CUDA(cudaStreamSynchronize(stream_));
   if (h != 0) {
     QFX_CUDA(cudaMemsetAsync(error_flag(), 0, sizeof(int), stream_));
-    throw QFX_ERR("A tensor-core pipeline wait expired (code ", h, "); results discarded.");
+    throw cat("ERROR (qflex_gb300: CUDA tensor-core pipeline) --> A tensor-core pipeline wait expired (code ", h,
+              "); results discarded.");
   }
 }
 

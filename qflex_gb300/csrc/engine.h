@@ -96,6 +96,8 @@ class Engine {
   int* error_flag();
   // Throws (and clears the flag) when a kernel reported an expired wait.
   void check_error_flag();
+  // Whether the error-flag buffer exists (a tensor-core kernel may have run).
+  bool has_error_flag() const { return (int)bufs_.size() > 5 && bufs_[5].ptr != nullptr; }
   // Split planes of the tensor-core products.
   float* tc_workspace(std::size_t elems);
   // C[m,n] = A[m,k] * B[k,n] (row-major complex64) in the context's
@@ -123,6 +125,7 @@ class Engine {
   int max_batch_ = 0;            // output strings per device pass (0: as many as fit)
   bool open_terminals_ = true;   // terminal cuts as open indices where the planner can
   bool fuse_splits_ = true;      // 3xFP16: permutes write the next product's A planes
+  unsigned long long wait_ns_ = 0;  // tensor-core pipeline wait limit (0: the kernels' 2 s)
   unsigned options_version_ = 0;  // part of the graph key: options change launches
   TcConfig tc_config(std::size_t m, std::size_t n, std::size_t k) const;
   // C = A * Bt^T on the tensor cores in the context's split precision.

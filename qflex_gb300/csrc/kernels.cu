@@ -225,6 +225,30 @@ __global__ void __launch_bounds__(256, 8) permute_kernel(const __grid_constant__
   }
 }
 
+// Index decomposition shared by the general permutation kernel and its host
+// mirror: the input offset of output element o.
+__host__ __device__ inline std::uint64_t general_source(const GeneralPerm& g, std::uint64_t o) {
+  std::uint64_t in = 0;
+  for (int i = int(g.rank) - 1; i >= 0; --i) {
+    const std::uint64_t d = g.out_dims[i];
+    const std::uint64_t q = o / d;
+    in += (o - q * d) * g.in_stride[i];
+    o = q;
+  }
+  return in;
+}
+
+__global__ void __launch_bounds__(256) permute_general_kernel(const __grid_constant__ GeneralPerm g,
+                                                              const float2* __restrict__ src,
+                                                              float2* __restrict__ dst,
+                                                              std::uint64_t batch_stride) {
+  const float2* s = src + std::uint64_t(blockIdx.y) * batch_stride;
+  float2* d = dst + std::uint64_t(blockIdx.y) * batch_stride;
+  for (std::uint64_t o = std::uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; o < g.size;
+       o += std::uint64_t(gridDim.x) * blockDim.x)
+    d[o] = __ldg(s + general_source(g, o));
+}
+
 // ---------------------------------------------------------------------------
 // Complex64 GEMM on CUDA cores (C = A * B, row-major).
 // Block tile BM x BN, k-step BK; each thread owns a TM x TN sub-tile.
@@ -643,6 +667,48 @@ void launch_permute(const PermPlan& plan, const float2* src, float2* dst, std::u
   dim3 grid(gx, (unsigned)batch, 1);
   permute_kernel<float2, false><<<grid, 256, 0, s>>>(plan, src, dst, batch_stride, PlaneOut{});
   check_launch("permute");
+}
+
+void make_general_perm(std::size_t rank, const std::size_t* dims, const std::size_t* new_order, GeneralPerm* g) {
+  if (rank > (std::size_t)kGeneralPermMaxRank)
+    throw std::string("ERROR (qflex_gb300: permute) --> at most 32 indices when a dimension is not a power of two");
+  std::memset(g, 0, sizeof(*g));
+  g->rank = (std::uint32_t)rank;
+  std::uint64_t stride[kGeneralPermMaxRank];
+  std::uint64_t size = 1;
+  for (std::size_t i = rank; i-- > 0;) {
+    if (dims[i] == 0) throw std::string("ERROR (qflex_gb300: permute) --> dimensions must be positive");
+    stride[i] = size;
+    if (dims[i] > (std::uint64_t(1) << 40) / size)
+      throw std::string("ERROR (qflex_gb300: permute) --> tensor exceeds 2^40 elements");
+    size *= dims[i];
+  }
+  bool seen[kGeneralPermMaxRank] = {};
+  for (std::size_t i = 0; i < rank; ++i) {
+    const std::size_t q = new_order[i];
+    if (q >= rank || seen[q]) throw std::string("ERROR (qflex_gb300: permute) --> new_order is not a permutation");
+    seen[q] = true;
+    g->out_dims[i] = dims[q];
+    g->in_stride[i] = stride[q];
+  }
+  g->size = size;
+}
+
+void permute_general_on_host(const GeneralPerm& g, const float2* src, float2* dst) {
+  for (std::uint64_t o = 0; o < g.size; ++o) {
+    const std::uint64_t at = general_source(g, o);
+    if (at >= g.size) throw std::string("ERROR (qflex_gb300: permute) --> load out of range");
+    dst[o] = src[at];
+  }
+}
+
+void launch_permute_general(const GeneralPerm& g, const float2* src, float2* dst, std::uint64_t batch_stride,
+                            int batch, cudaStream_t s) {
+  if (g.size == 0 || batch == 0) return;
+  const std::uint64_t blocks = std::min<std::uint64_t>((g.size + 255) / 256, 152ull * 64ull);
+  dim3 grid((unsigned)blocks, (unsigned)batch, 1);
+  permute_general_kernel<<<grid, 256, 0, s>>>(g, src, dst, batch_stride);
+  check_launch("permute_general");
 }
 
 void launch_permute64(const PermPlan& plan, const double2* src, double2* dst, std::uint64_t batch_stride,

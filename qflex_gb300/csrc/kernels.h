@@ -89,6 +89,27 @@ void launch_permute_fp16_planes(const PermPlan& plan, const float2* src, std::ui
                                 void* planes, int* exps, std::uint64_t rows, int k_log2, int batch,
                                 cudaStream_t s);
 
+// ---- permutation of indices of any dimension -------------------------------------
+// Output element o (row-major over the permuted dimensions) reads input
+// element sum_i digit_i(o) * in_stride[i], where in_stride[i] is the input
+// stride of the index that goes to position i. One thread per output
+// element: writes coalesced, reads gathered. For tensors whose dimensions
+// are not all powers of two.
+constexpr int kGeneralPermMaxRank = 32;
+struct GeneralPerm {
+  std::uint32_t rank;
+  std::uint64_t size;
+  std::uint64_t out_dims[kGeneralPermMaxRank];
+  std::uint64_t in_stride[kGeneralPermMaxRank];
+};
+// Throws (std::string) for a rank above kGeneralPermMaxRank, a zero
+// dimension, an element count above 2^40 or a new_order that is not a
+// permutation.
+void make_general_perm(std::size_t rank, const std::size_t* dims, const std::size_t* new_order, GeneralPerm* g);
+void permute_general_on_host(const GeneralPerm& g, const float2* src, float2* dst);
+void launch_permute_general(const GeneralPerm& g, const float2* src, float2* dst, std::uint64_t batch_stride,
+                            int batch, cudaStream_t s);
+
 // ---- complex64 products on CUDA cores -------------------------------------------
 // C[m,n] = A[m,k] * B[k,n], row-major, all three advanced by batch_stride
 // elements per batch entry. Products with m * n <= 64 and k >= 8192 split k

@@ -104,15 +104,23 @@ __device__ __forceinline__ bool mbar_test(std::uint64_t* bar, std::uint32_t pari
       : "memory");
   return ok != 0;
 }
+// Limit of a pipeline wait: the 64-bit value the host keeps after the error
+// code in the error-flag buffer (err[2..3], written when the buffer is
+// created and by the "tc_wait_ns" option), or WAIT_NS when it is 0. Read
+// only once a wait has to spin. The drains on the abort path keep WAIT_NS.
+__device__ __forceinline__ unsigned long long wait_limit_ns(const int* err) {
+  const unsigned long long v = *reinterpret_cast<const volatile unsigned long long*>(err + 2);
+  return v ? v : WAIT_NS;
+}
 // Bounded wait: false (and an error code) when the phase does not complete
-// within WAIT_NS or another warp of the CTA has already given up.
+// within the wait limit or another warp of the CTA has already given up.
 __device__ __forceinline__ bool mbar_wait(std::uint64_t* bar, std::uint32_t parity, volatile int* abort_flag,
                                           int* err, int code) {
   if (mbar_test(bar, parity)) return true;  // the common case reads no timer
-  const unsigned long long t0 = now_ns();
+  const unsigned long long t0 = now_ns(), limit = wait_limit_ns(err);
   while (!mbar_test(bar, parity)) {
     if (*abort_flag) return false;
-    if (now_ns() - t0 > WAIT_NS) {
+    if (now_ns() - t0 > limit) {
       *abort_flag = 1;
       atomicExch(err, code);
       return false;
@@ -307,10 +315,10 @@ __device__ __forceinline__ bool mbar_test_cluster(std::uint64_t* bar, std::uint3
 __device__ __forceinline__ bool mbar_wait_cluster(std::uint64_t* bar, std::uint32_t parity, volatile int* abort_flag,
                                                   int* err, int code) {
   if (mbar_test_cluster(bar, parity)) return true;
-  const unsigned long long t0 = now_ns();
+  const unsigned long long t0 = now_ns(), limit = wait_limit_ns(err);
   while (!mbar_test_cluster(bar, parity)) {
     if (*abort_flag) return false;
-    if (now_ns() - t0 > WAIT_NS) {
+    if (now_ns() - t0 > limit) {
       *abort_flag = 1;
       atomicExch(err, code);
       return false;

@@ -54,13 +54,14 @@ def test_fp64_paths_match_numpy_complex128(built_lib, ref_cases, name, precision
 
 def test_fp64_paths_on_the_16_slice_workload(built_lib):
     """Full 7x7 (1+32+1) workload, both cuts with 4 values (16 slices): the
-    float-float mode against the CPU complex128 oracle on every string of
-    tests/golden/c3_fp64.json, and against the native FP64 mode on one."""
+    float-float mode against the CPU complex128 oracle on the first four
+    strings of tests/golden/c3_fp64.json, and against the native FP64 mode
+    on one."""
     ref = json.loads((ROOT / "tests" / "golden" / "c3_fp64.json").read_text())
     circuit, ordering, grid, initial, finals = rqc.workload("c3")
     assert ref["initial"] == initial
-    strings = [r["final"] for r in ref["amplitudes"]]
-    want = [complex(*r["amplitude"]) for r in ref["amplitudes"]]
+    strings = [r["final"] for r in ref["amplitudes"][:4]]
+    want = [complex(*r["amplitude"]) for r in ref["amplitudes"][:4]]
     ff = Context(0, FP64_FF)
     got = [a for _, a in ff.evaluate_many(circuit, ordering, grid, initial, strings, 1 << 40)]
     assert _max_rel(got, want) < FP64_TOL

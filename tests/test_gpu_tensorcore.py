@@ -184,3 +184,45 @@ def test_tensorcore_multiply_batched(tc_ctx, extra):
         want = A @ B
         assert np.max(np.abs(C - want)) / np.mean(np.abs(want)) < 2e-5, b
         assert np.array_equal(out[b, m * k + k * n + m * n:], buf[b, m * k + k * n + m * n:])
+
+
+@pytest.mark.parametrize("precision", [FP16X3, TF32X3], ids=["fp16x3", "tf32x3"])
+def test_expired_pipeline_wait_is_reported_and_context_recovers(built_lib, precision):
+    """Every pipeline wait of the tensor-core kernels is bounded. With the
+    limit set to 1 ns the first wait that has to spin runs out: its thread
+    block drains what it started and returns, the call reports
+    QFLEX_GB300_ERR_CUDA, and with the default limit restored the same
+    context computes the same amplitudes and products as before."""
+    import torch
+
+    from qflex_gb300 import QflexGb300Error
+    circuit = rqc.random_circuit(6, 6, 24, seed=0)
+    grid = rqc.grid_text(6, 6)
+    ordering = rqc.ordering_6x6(cut_values=(1,))
+    finals = rqc.random_bitstrings(36, 2, 3)
+    ctx = Context(0, precision)
+    good = [a for _, a in ctx.evaluate_many(circuit, ordering, grid, "", finals, 1 << 40)]
+    g = np.random.default_rng(4)
+    m = n = k = 512
+    A = torch.from_numpy((g.standard_normal((m, k)) + 1j * g.standard_normal((m, k))).astype(np.complex64)).cuda()
+    B = torch.from_numpy((g.standard_normal((k, n)) + 1j * g.standard_normal((k, n))).astype(np.complex64)).cuda()
+    C = torch.zeros((m, n), dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()
+
+    ctx.set_option("tc_wait_ns", 1)
+    assert ctx.get_option("tc_wait_ns") == 1
+    with pytest.raises(QflexGb300Error) as e:
+        ctx.evaluate_many(circuit, ordering, grid, "", finals, 1 << 40)
+    assert e.value.code == 2 and "pipeline wait expired" in str(e.value)
+    ctx.multiply(A.data_ptr(), B.data_ptr(), C.data_ptr(), m, n, k)
+    with pytest.raises(QflexGb300Error) as e:
+        ctx.synchronize()
+    assert e.value.code == 2 and "pipeline wait expired" in str(e.value)
+
+    ctx.set_option("tc_wait_ns", 0)
+    again = [a for _, a in ctx.evaluate_many(circuit, ordering, grid, "", finals, 1 << 40)]
+    assert again == good
+    ctx.multiply(A.data_ptr(), B.data_ptr(), C.data_ptr(), m, n, k)
+    ctx.synchronize()
+    want = A.cpu().numpy().astype(np.complex128) @ B.cpu().numpy().astype(np.complex128)
+    assert np.max(np.abs(C.cpu().numpy() - want)) < 2e-5 * np.mean(np.abs(want))
