@@ -178,6 +178,75 @@ def workload(name: str, seed: int = 0):
     return circuit, ordering, grid_text(I, J), initial, finals
 
 
+# ---- fSim circuits on a rectangular grid ----------------------------------
+
+FSIM_PATTERNS = "ABCDCDAB"  # coupler pattern of cycle c is FSIM_PATTERNS[(c - 1) % 8]
+
+
+def fsim_pattern_pairs(I: int, J: int, pattern: str, off: Iterable[Coord] = ()) -> List[Tuple[Coord, Coord]]:
+    """Couplers of one of the four alternating patterns on an I x J grid:
+    A horizontal (i, j)-(i, j+1) with j even, B the same with j odd, C
+    vertical (i, j)-(i+1, j) with i even, D the same with i odd. Couplers
+    touching an off site are left out. Every coupler of the grid belongs to
+    exactly one pattern."""
+    off = set(map(tuple, off))
+    pairs = []
+    if pattern in "AB":
+        par = 0 if pattern == "A" else 1
+        pairs = [((i, j), (i, j + 1)) for i in range(I) for j in range(J - 1) if j % 2 == par]
+    elif pattern in "CD":
+        par = 0 if pattern == "C" else 1
+        pairs = [((i, j), (i + 1, j)) for i in range(I - 1) if i % 2 == par for j in range(J)]
+    else:
+        raise ValueError(pattern)
+    return [(a, b) for a, b in pairs if a not in off and b not in off]
+
+
+def random_off_site(I: int, J: int, seed: int) -> Coord:
+    """One disabled site drawn from the grid's interior (seeded)."""
+    rng = np.random.default_rng(seed)
+    return (int(rng.integers(1, I - 1)), int(rng.integers(1, J - 1)))
+
+
+def fsim_circuit(I: int, J: int, cycles: int, seed: int, off: Iterable[Coord] = (),
+                 theta: float = 0.5, phi: float = 1.0 / 6.0, jitter_rad: float = 0.05) -> str:
+    """Circuit text of an fSim random circuit: cycle c (1..cycles) is a layer
+    of single-qubit gates on every active qubit at time 2c - 1, drawn
+    uniformly from {x_1_2, y_1_2, hz_1_2} minus the qubit's previous one, and
+    fSim(theta, phi + jitter) on the couplers of pattern
+    FSIM_PATTERNS[(c - 1) % 8] at time 2c; a last single-qubit layer follows
+    at time 2 cycles + 1. Angles are in units of pi, as the circuit format
+    gives them (src/read_circuit.cpp:157-158); every coupler draws its own
+    phase jitter once, from N(0, jitter_rad) radians. Each fSim splits into
+    two tensors joined by a bond of dimension 4, so a coupler that gets g
+    fSims carries a bond of 4^g."""
+    rng = np.random.default_rng(seed)
+    off = set(map(tuple, off))
+    active = [(i, j) for i in range(I) for j in range(J) if (i, j) not in off]
+    q = {p: p[0] * J + p[1] for p in active}
+    jitter = {}
+    for pat in "ABCD":
+        for pair in fsim_pattern_pairs(I, J, pat, off):
+            jitter[pair] = rng.normal(0.0, jitter_rad) / np.pi
+    names = ["x_1_2", "y_1_2", "hz_1_2"]
+    last = {p: None for p in active}
+    lines = [str(len(active))]
+
+    def single_layer(t):
+        for p in active:
+            choices = [g for g in names if g != last[p]]
+            g = choices[int(rng.integers(len(choices)))]
+            last[p] = g
+            lines.append(f"{t} {g} {q[p]}")
+
+    for c in range(1, cycles + 1):
+        single_layer(2 * c - 1)
+        for a, b in fsim_pattern_pairs(I, J, FSIM_PATTERNS[(c - 1) % 8], off):
+            lines.append(f"{2 * c} fsim({theta!r}, {phi + jitter[(a, b)]!r}) {q[a]} {q[b]}")
+    single_layer(2 * cycles + 1)
+    return "\n".join(lines) + "\n"
+
+
 # Real flop (8 m n k summed over the complex products) of one amplitude of
 # the c3 workload, keyed by the number of cut slices summed: 16 for the
 # workload's ordering, 4 for ordering_7x7((0,), (0, 1, 2, 3)) and 1 for
