@@ -123,10 +123,11 @@ size_t qflex_gb300_last_ops(const qflex_gb300_context* ctx, double* out, size_t 
 
 /* Tuning options of a context; no reference counterpart (the reference has
  * no device kernels to tune). Names and values:
- *   "tc_chunk"   k-steps of 8 per TMEM accumulation chunk of the split
- *                tensor-core product, 1..64 (default 2, or QFLEX_TC_CHUNK;
+ *   "tc_chunk"   k-steps per TMEM accumulation chunk of the split
+ *                tensor-core product, 1..64 (default 1, or QFLEX_TC_CHUNK;
  *                longer chunks are faster and less accurate: the tensor
- *                core's FP32 accumulation truncates)
+ *                core's FP32 accumulation truncates, which shrinks every
+ *                product by an amount that grows with the chunk)
  *   "tc_pair"    1: 3xTF32 products with m >= 256 use the CTA-pair
  *                (cta_group::2, 256 x 128 tile) kernel; 0: every product uses
  *                the single-CTA 128 x 128 tile (default 0, or QFLEX_TC_PAIR)
@@ -139,6 +140,10 @@ size_t qflex_gb300_last_ops(const qflex_gb300_context* ctx, double* out, size_t 
  *                planes (scaled per 32 values of a row) directly instead of
  *                complex64, and the product skips splitting A (default 1,
  *                or QFLEX_GB300_FUSE)
+ *   "exact_gates" -1: the plain FP32 path builds its gate tensors from the
+ *                reference's float gate constants, every other mode from double
+ *                constants (default); 1: every mode from double constants; 0:
+ *                every complex64 mode from float constants
  *   "tc_wait_ns" limit in ns of every pipeline wait of the tensor-core
  *                products (0: 2 s, the default). A wait that runs out stops its
  *                thread block, which drains the copies and MMAs it started,

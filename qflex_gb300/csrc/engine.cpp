@@ -133,6 +133,9 @@ void Engine::set_option(const std::string& name, double value) {
   } else if (name == "open_terminals") {
     if (value != 0 && value != 1) throw QFX_ERR("Option open_terminals must be 0 or 1.");
     open_terminals_ = value != 0;
+  } else if (name == "exact_gates") {
+    if (value != -1 && value != 0 && value != 1) throw QFX_ERR("Option exact_gates must be -1, 0 or 1.");
+    exact_gates_ = int(value);
   } else if (name == "tc_wait_ns") {
     if (!(value >= 0 && value <= 1e11) || value != double((unsigned long long)value))
       throw QFX_ERR("Option tc_wait_ns must be an integer in 0..1e11.");
@@ -160,6 +163,7 @@ double Engine::get_option(const std::string& name) const {
   if (name == "open_terminals") return open_terminals_ ? 1 : 0;
   if (name == "fuse_splits") return fuse_splits_ ? 1 : 0;
   if (name == "tc_wait_ns") return double(wait_ns_);
+  if (name == "exact_gates") return exact_gates_;
   throw QFX_ERR("Unknown option '", name, "'.");
 }
 
@@ -291,6 +295,7 @@ Engine::Plan* Engine::get_plan(const std::string& circuit, const std::string& or
   key += '\x01';
   key += std::to_string(precision_);
   key += open_terminals_ ? "o" : "p";
+  key += std::to_string(exact_gates_);
   if (plan_ && plan_->key == key) return plan_.get();
   auto p = std::make_unique<Plan>();
   p->key = std::move(key);
@@ -594,7 +599,7 @@ std::vector<EvalResult> Engine::evaluate(const std::string& circuit, const std::
     // split-precision path evaluates the columns from double constants (in
     // float-float), the complex128 path in FP64.
     const bool wide = is_complex128(precision_);
-    const bool exact_gates = precision_ != FP32;
+    const bool exact_gates = exact_gates_ < 0 ? precision_ != FP32 : exact_gates_ != 0;
     build_flatten_tables(p.net, p.prog, exact_gates, &cols, &steps, &mats, &mats_lo, wide ? &mats64 : nullptr,
                          &p.max_size_log2);
     std::vector<std::uint32_t> ptr(p.prog.n_amplitudes + 1, 0), leaves(p.prog.n_leaves);

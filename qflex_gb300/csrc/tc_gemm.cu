@@ -1422,9 +1422,12 @@ unsigned persistent_grid(std::size_t tiles) {
 
 TcConfig tc_default_config() {
   TcConfig c;
-  // k-steps per TMEM chunk. Measured on the 7x7 (1+32+1) network (8
-  // amplitudes vs FP64): 1 -> max 1.0e-5 at 8.9 amplitudes/s, 2 -> max
-  // 8.7e-6 at 9.8, 4 -> max 1.6e-5 at 10.4.
+  // k-steps per TMEM chunk. The tensor core's FP32 accumulation truncates,
+  // which shrinks every product by a few 1e-8 per truncating add; a chunk's
+  // adds are the unit of that bias. Measured on 256 amplitudes of the 16-slice
+  // 7x7 (1+32+1) workload against the FP64 oracle (3xFP16): chunk 2 shrinks
+  // every amplitude by 4.9e-6 (largest error 1.1e-5 of the RMS amplitude),
+  // chunk 1 by 2.2e-6 (5.6e-6) at 7 % less throughput.
   if (const char* e = std::getenv("QFLEX_TC_CHUNK")) {
     const int v = std::atoi(e);
     if (v >= 1 && v <= 64) c.chunk = v;

@@ -247,6 +247,53 @@ def fsim_circuit(I: int, J: int, cycles: int, seed: int, off: Iterable[Coord] = 
     return "\n".join(lines) + "\n"
 
 
+def ordering_6x9(off: Coord, cut_values: Optional[Sequence[int]] = (0, 1), terminal_region: bool = True) -> str:
+    """Column sweep of a 6 x 9 grid (one site off): columns 0-3 are
+    contracted first (patch P, shared by every cut value), then three cuts on
+    the couplers (0,4)-(0,5), (1,4)-(1,5), (2,4)-(2,5), each taking
+    `cut_values` (None: all values), then P continues column by column. The
+    six qubits of column 8 form the output region: with ``terminal_region``
+    they are terminal cuts, so one contraction yields the region's 64
+    amplitudes. Every cut precedes the expansion of its tensors and every
+    merge goes into a patch created after the last cut, as the reference
+    requires (src/contraction_utils.cpp:534-610)."""
+    I, J = 6, 9
+
+    def col(j):
+        return [(i, j) for i in range(I) if (i, j) != tuple(off)]
+
+    L = [f"expand P {i * J + j}" for j in range(4) for i, _ in col(j)]
+    for i in range(3):
+        L.append(f"cut {_vals(cut_values)} {i * J + 4} {i * J + 5}")
+    if terminal_region:
+        L += [f"cut () {i * J + 8}" for i, _ in col(8)]
+    L.append("merge P L")
+    L += [f"expand L {i * J + j}" for j in range(4, J) for i, _ in col(j)]
+    return "\n".join(L) + "\n"
+
+
+def workload_c4(seed: int = 0, cycles: int = 8, n_prefixes: int = 64):
+    """The fSim workload: 6 x 9 grid with one seeded disabled site (53 active
+    qubits), fsim_circuit(cycles) with fSim(pi/2, pi/6 + N(0, 0.05) rad),
+    ordering_6x9 (3 cuts x 2 values = 8 slices) and `n_prefixes` random
+    output strings whose last-column region is open ('x'): each gives the 64
+    amplitudes of the strings that share its 47 other bits (4096 amplitudes
+    for 64 prefixes). At 8 cycles every coupler carries 2 fSims (bond 16);
+    20 cycles would put 5 on each (bond 1024, grid tensors of up to 2^40
+    elements), which no grid contraction can hold."""
+    I, J = 6, 9
+    off = random_off_site(I, J, seed + 7)
+    circuit = fsim_circuit(I, J, cycles, seed, off=[off])
+    grid = grid_text(I, J, [off])
+    ordering = ordering_6x9(off)
+    active = [(i, j) for i in range(I) for j in range(J) if (i, j) != off]
+    region = {k for k, p in enumerate(active) if p[1] == 8}
+    initial = random_bitstrings(len(active), 1, seed + 1)[0]
+    finals = ["".join("x" if k in region else b for k, b in enumerate(f))
+              for f in random_bitstrings(len(active), n_prefixes, seed + 2)]
+    return circuit, ordering, grid, initial, finals
+
+
 # Real flop (8 m n k summed over the complex products) of one amplitude of
 # the c3 workload, keyed by the number of cut slices summed: 16 for the
 # workload's ordering, 4 for ordering_7x7((0,), (0, 1, 2, 3)) and 1 for
