@@ -41,3 +41,11 @@ def rel_err(got, want):
     w = np.asarray(want, dtype=np.complex128)
     scale = max(float(np.sqrt(np.mean(np.abs(w) ** 2))), 1e-300)
     return float(np.max(np.abs(g - w))) / scale
+
+
+def rel_err_per_amplitude(got, want):
+    """Largest |got - want| / |want| over the set, amplitude by amplitude."""
+    import numpy as np
+    g = np.asarray(got, dtype=np.complex128)
+    w = np.asarray(want, dtype=np.complex128)
+    return float(np.max(np.abs(g - w) / np.abs(w)))

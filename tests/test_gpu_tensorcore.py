@@ -226,3 +226,44 @@ def test_expired_pipeline_wait_is_reported_and_context_recovers(built_lib, preci
     ctx.synchronize()
     want = A.cpu().numpy().astype(np.complex128) @ B.cpu().numpy().astype(np.complex128)
     assert np.max(np.abs(C.cpu().numpy() - want)) < 2e-5 * np.mean(np.abs(want))
+
+
+
+def test_split_paths_per_amplitude_on_the_16_slice_workload(built_lib):
+    """The full 7x7 (1+32+1) workload (two cuts x 4 values, 16 slices).
+    Every split precision: each of the 16 amplitudes of
+    tests/golden/c3_fp64.json (CPU complex128 oracle) within 1e-5 of it.
+    The default 3xFP16 path on the 256 strings of
+    tests/golden/c3_fp64_gpu.json (GPU complex128 oracle): every amplitude
+    within 1e-5 of the RMS amplitude, the systematic shrink from the tensor
+    core's truncating accumulation below 3e-6, and at least 95 % of the
+    amplitudes within 1e-5 of themselves (the rest are the smallest
+    amplitudes, down to 0.05 of the RMS, whose relative error complex64
+    arithmetic cannot hold to 1e-5: the FP32 CUDA-core path's largest is
+    5.5e-5 on the same strings)."""
+    import json
+
+    from tests.conftest import ROOT, rel_err_per_amplitude
+    circuit, ordering, grid, initial, finals = rqc.workload("c3")
+    cpu = json.loads((ROOT / "tests" / "golden" / "c3_fp64.json").read_text())
+    strings = [r["final"] for r in cpu["amplitudes"]]
+    want = [complex(*r["amplitude"]) for r in cpu["amplitudes"]]
+    assert len(strings) >= 16
+    for precision in (TF32X3, FP16X3, BF16X3):
+        ctx = Context(0, precision)
+        got = [a for _, a in ctx.evaluate_many(circuit, ordering, grid, initial, strings, 1 << 40)]
+        assert rel_err_per_amplitude(got, want) < TOL, precision
+        ctx.close()
+    gpu = json.loads((ROOT / "tests" / "golden" / "c3_fp64_gpu.json").read_text())
+    strings = [r["final"] for r in gpu["amplitudes"]]
+    want = np.array([complex(*r["amplitude"]) for r in gpu["amplitudes"]])
+    ctx = Context(0, FP16X3)
+    got = []
+    for i in range(0, len(strings), 8):
+        got += [a for _, a in ctx.evaluate_many(circuit, ordering, grid, initial, strings[i:i + 8], 1 << 40)]
+    got = np.array(got)
+    rms = np.sqrt(np.mean(np.abs(want) ** 2))
+    per_amp = np.abs(got - want) / np.abs(want)
+    assert np.max(np.abs(got - want)) / rms < TOL
+    assert abs(np.mean((got / want).real) - 1) < 3e-6
+    assert np.mean(per_amp <= TOL) >= 0.95 and np.max(per_amp) < 3e-5
