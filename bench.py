@@ -52,6 +52,9 @@ def parse():
     p.add_argument("--batch", type=int, default=8, help="output strings per step")
     p.add_argument("--impl", default="engine", choices=["engine", "reference"])
     p.add_argument("--precision", default="fp16x3", choices=["fp16x3", "tf32x3", "bf16x3", "fp32"])
+    p.add_argument("--ordering", default="learned", choices=["learned", "supplied"],
+                   help="the cost model's ordering of the workload (qflex_gb300/orderings/c3_learned.txt) or the "
+                        "supplied one; both sum the same cut slices")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-autotune", action="store_true",
                    help="skip the tensor-core kernel / strings-per-pass autotuning before warm-up")
@@ -223,7 +226,7 @@ def run_reference(args, rank):
 def config(args):
     return {"workload": "7x7 grid RQC depth (1+32+1), 49 qubits, CZ bond 16, two cuts x 4 values "
                         "(16 slices), random 49-bit output strings",
-            "strings_per_step": args.batch, "precision": args.precision,
+            "strings_per_step": args.batch, "precision": args.precision, "ordering": args.ordering,
             "parallelism": f"replicas{args.gpus}",
             "l2": "inputs larger than L2 (1.1 GB HBM arena per output string)"}
 
@@ -427,6 +430,8 @@ def main():
     ctx.set_precision(args.precision)
     ctx.set_stream(stream.cuda_stream)
     circuit, ordering, grid, initial, finals = rqc.workload(WORKLOAD)
+    if args.ordering == "learned":
+        ordering = rqc.ordering_7x7_learned()
     B = args.batch
 
     def strings(step):

@@ -117,6 +117,96 @@ def candidate_orderings(I: int, J: int, count: Optional[int] = None, seed: int =
     return out
 
 
+def _rect_sweep(rows: Sequence[int], cols: Sequence[int], col_major: bool, rev_outer: bool, rev_inner: bool,
+                snake: bool) -> List[Tuple[int, int]]:
+    """Cells of a rectangle swept line by line: rows (or columns with
+    ``col_major``), each direction optionally reversed, snaking or not.
+    Every cell after the first touches an earlier one."""
+    outer, inner = (list(cols), list(rows)) if col_major else (list(rows), list(cols))
+    if rev_outer:
+        outer.reverse()
+    seq = []
+    for t, o in enumerate(outer):
+        line = list(reversed(inner)) if (rev_inner ^ (snake and t % 2 == 1)) else list(inner)
+        seq += [(i, o) if col_major else (o, i) for i in line]
+    return seq
+
+
+def sweep_candidates_7x7(cut1_values: Optional[Sequence[int]], cut2_values: Optional[Sequence[int]],
+                         count: int = 500, seed: int = 0) -> List[Candidate]:
+    """Seeded random row and column sweep variants of the 7x7 grid ordering
+    of rqc.ordering_7x7: the same patches (A, pB, ppD, B, pD, pC, D, C), the
+    same two cuts with the same values and the same merges, and in every
+    patch a sweep drawn at random: each rectangle swept by rows or by
+    columns from its corner on the grid's edge, snaking or not (the single
+    lines grow from the cuts outwards). 1024 variants exist.
+    All candidates sum the same cut slices, so they give the same
+    amplitudes; they differ in product shapes (so in flop), in the
+    permutations between products and in memory. Duplicates are dropped."""
+    rng = np.random.default_rng(seed)
+
+    def q(c):
+        return c[0] * 7 + c[1]
+
+    def rect(rows, cols):
+        # Starts at the rectangle's first (row, column) corner, as listed:
+        # rows and cols are given from the grid's outside inwards.
+        return _rect_sweep(rows, cols, bool(rng.integers(2)), False, False, bool(rng.integers(2)))
+
+    out, seen = [], set()
+    tries = 0
+    while len(out) < count and tries < 50 * count:
+        tries += 1
+        A = rect(range(0, 3), range(0, 3))
+        pB = rect(range(6, 2, -1), range(0, 2))
+        ppD = rect(range(6, 3, -1), range(6, 3, -1))
+        # Single lines grow from the cut outwards, as in rqc.ordering_7x7:
+        # the other direction holds tensors of more than 2^31 elements.
+        Bc = [(r, 2) for r in range(6, 2, -1)]
+        pDc = [(r, 3) for r in range(6, 3, -1)]
+        pC = rect(range(0, 3), range(6, 4, -1))
+        Dr = [(3, c) for c in range(6, 2, -1)]
+        # Region cells: column 4 before column 3 in each row (connectivity).
+        region = rect(range(0, 3), (4, 3))
+        L = [f"expand A {q(c)}" for c in A] + [f"expand pB {q(c)}" for c in pB] + \
+            [f"expand ppD {q(c)}" for c in ppD]
+        L.append(f"cut {_vals(cut1_values)} {q((6, 2))} {q((6, 3))}")
+        L.append("merge pB B")
+        L += [f"expand B {q(c)}" for c in Bc]
+        L.append("merge A B")
+        L.append("merge ppD pD")
+        L += [f"expand pD {q(c)}" for c in pDc]
+        L.append(f"cut {_vals(cut2_values)} {q((2, 6))} {q((3, 6))}")
+        L += [f"expand pC {q(c)}" for c in pC]
+        L.append("merge pD D")
+        L += [f"expand D {q(c)}" for c in Dr]
+        L.append("merge B D")
+        L.append("merge pC C")
+        L += [f"expand C {q(c)}" for c in region]
+        L.append("merge D C")
+        text = "\n".join(L) + "\n"
+        if text in seen:
+            continue
+        seen.add(text)
+        out.append(Candidate(text, f"sweep#{len(out)}"))
+    return out
+
+
+def _vals(values: Optional[Sequence[int]]) -> str:
+    return "(" + ",".join(str(v) for v in values) + ")" if values else "()"
+
+
+def auto_orderer_cost(ops: np.ndarray) -> float:
+    """The reference auto-orderer's cost of a plan: the sum over its
+    contractions of 2^op_size, op_size = log2 of (m k) + (k n) - k... i.e.
+    rank(A) - d + rank(B) - d + d for two tensors sharing a bond of 2^d
+    (qflexcirq/ordering/order_circuit_simulation.py:87-106), which is m n k
+    of the product. Permutations cost nothing in it."""
+    ops = np.asarray(ops, dtype=np.float64).reshape(-1, 8)
+    prod = ops[:, 0] != 0
+    return float((ops[prod, 1] * ops[prod, 2] * ops[prod, 3]).sum())
+
+
 # ---------------------------------------------------------------------------
 # The perceptron (kernels in libqflex_gb300.so).
 # ---------------------------------------------------------------------------
@@ -262,3 +352,147 @@ def choose_ordering(model: CostModel, circuit: str, grid: str, candidates: Seque
         if t < best[0]:
             best = (t, cand.text, cand.label)
     return best
+
+
+# ---------------------------------------------------------------------------
+# The search: candidates ranked by the learned model and by the baselines,
+# the picks measured.
+# ---------------------------------------------------------------------------
+
+def _spearman(a, b) -> float:
+    ra = np.argsort(np.argsort(a))
+    rb = np.argsort(np.argsort(b))
+    return float(np.corrcoef(ra, rb)[0, 1])
+
+
+def run_search(circuit: str, grid: str, supplied: str, candidates: Sequence[Candidate], finals: Sequence[str],
+               precision: int, n_train: int = 12, n_sample: int = 20, memory_limit: float = 180e9,
+               seed: int = 0, repeats: int = 2, log=print) -> dict:
+    """Plans every candidate (planning only; those beyond the memory limit
+    or the 2^31-element tensor limit drop out), profiles `n_train` of them
+    op by op on the GPU, fits the cost model on those timings, and ranks the
+    rest by three costs: the model's predicted time, the reference
+    auto-orderer's sum of m n k (auto_orderer_cost) and the roofline
+    estimate (analytic_ms). Each ranking's pick is measured, with the
+    supplied ordering and `n_sample` held-out candidates for the rank
+    correlations. Amplitudes of every measured ordering are compared with
+    the supplied ordering's. Returns a report (dict)."""
+    from ._lib import Context
+    batch = len(finals)
+    rng = np.random.default_rng(seed)
+    plans = []
+    for cand in candidates:
+        try:
+            ops, arena = plan_ops(circuit, cand.text, grid, precision, batch)
+        except QflexGb300Error:
+            continue
+        if arena * batch > memory_limit:
+            continue
+        plans.append((cand, ops))
+    log(f"{len(plans)} of {len(candidates)} candidates plan within the limits")
+    order = rng.permutation(len(plans))
+    train = [plans[i] for i in order[:n_train]]
+    held = [plans[i] for i in order[n_train:]]
+    ctx = Context(0, precision)
+    feats, times = [], []
+    ref_amps = None
+    for cand, _ in train:
+        ops, _, amps = profile(ctx, circuit, cand.text, grid, finals, repeats=repeats)
+        feats.append(op_features(ops))
+        times.append(ops[:, 7])
+    model = CostModel(hidden=64, seed=seed)
+    model.fit(np.vstack(feats), np.concatenate(times), epochs=1500)
+    pred = np.array([model.predict_plan_ms(ops) for _, ops in held])
+    auto = np.array([auto_orderer_cost(ops) for _, ops in held])
+    roof = np.array([analytic_ms(ops) for _, ops in held])
+
+    def measure(text):
+        ctx.evaluate_many(circuit, text, grid, "", list(finals), memory_limit)
+        best, out = float("inf"), None
+        for _ in range(repeats):
+            out = ctx.evaluate_many(circuit, text, grid, "", list(finals), memory_limit)
+            best = min(best, ctx.stats()["device_ms"])
+        return best, [a for _, a in out]
+
+    t_sup, ref_amps = measure(supplied)
+
+    def rel(amps):
+        g = np.asarray(amps)
+        w = np.asarray(ref_amps)
+        return float(np.max(np.abs(g - w)) / np.sqrt(np.mean(np.abs(w) ** 2)))
+
+    picks = {}
+    for name, score in (("model", pred), ("auto_orderer", auto), ("roofline", roof)):
+        i = int(np.argmin(score))  # ties go to the first candidate in list order
+        t, amps = measure(held[i][0].text)
+        picks[name] = {"label": held[i][0].label, "index": i, "measured_ms": t, "amplitude_err_vs_supplied": rel(amps),
+                       "gemm_flop": float(held[i][1][:, 4].sum()),
+                       "permute_bytes": float(held[i][1][held[i][1][:, 0] == 0, 5].sum())}
+        log(f"{name} pick {held[i][0].label}: {t:.1f} ms")
+    sample = rng.choice(len(held), size=min(n_sample, len(held)), replace=False)
+    measured = []
+    for i in sample:
+        t, amps = measure(held[i][0].text)
+        measured.append(t)
+        assert rel(amps) < 1e-4, held[i][0].label
+    measured = np.array(measured)
+    # Regret of each ranking on random subsets of the measured sample: the
+    # measured time of the subset's pick over the subset's best.
+    regret = {}
+    subsets = [rng.choice(len(sample), size=min(8, len(sample)), replace=False) for _ in range(2000)]
+    for name, score in (("model", pred[sample]), ("auto_orderer", auto[sample]), ("roofline", roof[sample])):
+        r = [measured[sub[int(np.argmin(score[sub]))]] / measured[sub].min() - 1.0 for sub in subsets]
+        regret[name] = float(np.mean(r))
+    disagree = [sub for sub in subsets if int(np.argmin(pred[sample][sub])) != int(np.argmin(auto[sample][sub]))]
+    faster = sum(measured[sub[int(np.argmin(pred[sample][sub]))]] < measured[sub[int(np.argmin(auto[sample][sub]))]]
+                 for sub in disagree)
+    return {
+        "candidates": len(candidates), "planned": len(plans), "trained_on": len(train), "held_out": len(held),
+        "strings": batch, "supplied_ms": t_sup, "picks": picks,
+        "sample": {"size": int(len(sample)), "best_ms": float(measured.min()), "worst_ms": float(measured.max()),
+                   "spearman": {"model": _spearman(pred[sample], measured),
+                                "auto_orderer": _spearman(auto[sample], measured),
+                                "roofline": _spearman(roof[sample], measured)},
+                   "mean_regret_8_of_sample": regret,
+                   "subsets_where_model_and_auto_orderer_disagree": len(disagree),
+                   "of_those_model_pick_faster": int(faster)},
+        "model_text": held[picks["model"]["index"]][0].text,
+    }
+
+
+def main(argv=None) -> None:
+    """python -m qflex_gb300.learned --depth 40 [--slices 1] [--count 500] --out report.json"""
+    import argparse
+    import json
+
+    from . import rqc
+    from ._lib import PRECISIONS
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--depth", type=int, default=40)
+    ap.add_argument("--values", type=int, default=1, help="values per cut (slices = values^2)")
+    ap.add_argument("--count", type=int, default=500)
+    ap.add_argument("--strings", type=int, default=1)
+    ap.add_argument("--train", type=int, default=12)
+    ap.add_argument("--sample", type=int, default=20)
+    ap.add_argument("--precision", default="fp16x3")
+    ap.add_argument("--memory", type=float, default=180e9)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--out", required=True)
+    args = ap.parse_args(argv)
+    circuit = rqc.random_circuit(7, 7, args.depth, seed=0)
+    grid = rqc.grid_text(7, 7)
+    vals = tuple(range(args.values))
+    supplied = rqc.ordering_7x7(vals, vals)
+    finals = rqc.random_bitstrings(49, args.strings, 2)
+    cands = sweep_candidates_7x7(vals, vals, count=args.count, seed=args.seed)
+    rep = run_search(circuit, grid, supplied, cands, finals, PRECISIONS[args.precision], n_train=args.train,
+                     n_sample=args.sample, memory_limit=args.memory, seed=args.seed)
+    rep.update({"workload": f"7x7 grid, depth (1+{args.depth}+1), 2 cuts x {args.values} values",
+                "precision": args.precision})
+    with open(args.out, "w") as f:
+        json.dump(rep, f, indent=1)
+    print(json.dumps({k: v for k, v in rep.items() if k != "model_text"}, indent=1))
+
+
+if __name__ == "__main__":
+    main()

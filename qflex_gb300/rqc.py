@@ -303,6 +303,14 @@ def workload_c4(seed: int = 0, cycles: int = 8, n_prefixes: int = 64):
 C3_GEMM_FLOP = {16: 14910827790336.0, 4: 3964990390272.0, 1: 1772918145024.0}
 
 
+def ordering_7x7_learned() -> str:
+    """The learned cost model's choice for the c3 workload (same cuts and
+    values as ordering_7x7((0, 1, 2, 3), (0, 1, 2, 3)), so the same
+    amplitudes), kept in orderings/c3_learned.txt."""
+    from pathlib import Path
+    return (Path(__file__).resolve().parent / "orderings" / "c3_learned.txt").read_text()
+
+
 def ordering_6x6(cut_values: Optional[Sequence[int]] = None) -> str:
     """6x6: cut the vertical bond (2,3)-(3,3) first, contract the top half
     (rows 0-2) and the bottom half (rows 5..3) as two patches, row by row
