@@ -124,13 +124,16 @@ size_t qflex_gb300_last_ops(const qflex_gb300_context* ctx, double* out, size_t 
 /* Tuning options of a context; no reference counterpart (the reference has
  * no device kernels to tune). Names and values:
  *   "tc_chunk"   k-steps per TMEM accumulation chunk of the split
- *                tensor-core product, 1..64 (default 1, or QFLEX_TC_CHUNK;
+ *                tensor-core product, 1..64 (default 2, or QFLEX_TC_CHUNK;
  *                longer chunks are faster and less accurate: the tensor
  *                core's FP32 accumulation truncates, which shrinks every
  *                product by an amount that grows with the chunk)
  *   "tc_pair"    1: 3xTF32 products with m >= 256 use the CTA-pair
  *                (cta_group::2, 256 x 128 tile) kernel; 0: every product uses
  *                the single-CTA 128 x 128 tile (default 0, or QFLEX_TC_PAIR)
+ *   "tc_variant" tensor-core kernel of every product without a per-shape
+ *                choice (qflex_gb300_set_tc_variant): 0..3 as listed there
+ *                (default 0; "tc_pair" sets 0 or the pair-for-m >= 256 rule)
  *   "graphs"     1: capture a repeated device pass in a CUDA graph and
  *                replay it (default 1, or QFLEX_GB300_GRAPHS)
  *   "max_batch"  most output strings per device pass of evaluate_many
@@ -140,6 +143,12 @@ size_t qflex_gb300_last_ops(const qflex_gb300_context* ctx, double* out, size_t 
  *                planes (scaled per 32 values of a row) directly instead of
  *                complex64, and the product skips splitting A (default 1,
  *                or QFLEX_GB300_FUSE)
+ *   "tc_debias"  1: the split tensor-core products multiply their outputs
+ *                by 1 + beta, the mean fraction the tensor core's truncating
+ *                accumulation loses (measured on GB300 per split kind for
+ *                chunks of 1 and 2 k-steps on Gaussian operands; other
+ *                chunk lengths are not compensated); 0: no compensation
+ *                (default 1)
  *   "exact_gates" -1: the plain FP32 path builds its gate tensors from the
  *                reference's float gate constants, every other mode from double
  *                constants (default); 1: every mode from double constants; 0:
@@ -161,8 +170,10 @@ int qflex_gb300_set_option(qflex_gb300_context* ctx, const char* name, double va
 int qflex_gb300_get_option(const qflex_gb300_context* ctx, const char* name, double* value);
 /* Tensor-core kernel for products of shape (m, n, k), e.g. chosen by an
  * autotuner: 0 single CTA, 1 CTA pair (needs m >= 64), 2 single CTA with a
- * deeper operand pipeline (3xFP16; the other precisions take 0), -1 removes
- * the override. Overrides "tc_pair" for that shape. */
+ * deeper operand pipeline (3xFP16), 3 single CTA with 16 epilogue warps
+ * (3xFP16; outputs that cannot take bulk tensor stores use 0); the other
+ * precisions take 0. -1 removes the override. Overrides "tc_pair" for that
+ * shape. */
 int qflex_gb300_set_tc_variant(qflex_gb300_context* ctx, size_t m, size_t n, size_t k, int variant);
 
 /* ---- tensor-level operations on device memory (complex64, interleaved) ----

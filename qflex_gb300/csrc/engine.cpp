@@ -121,6 +121,10 @@ void Engine::set_option(const std::string& name, double value) {
     if (!(value >= 1 && value <= 64) || value != double(int(value)))
       throw QFX_ERR("Option tc_chunk must be an integer in 1..64.");
     tc_cfg_.chunk = int(value);
+  } else if (name == "tc_variant") {
+    if (!(value >= 0 && value <= 3) || value != double(int(value)))
+      throw QFX_ERR("Option tc_variant must be 0, 1, 2 or 3.");
+    tc_cfg_.variant = int(value);
   } else if (name == "tc_pair") {
     if (value != 0 && value != 1) throw QFX_ERR("Option tc_pair must be 0 or 1.");
     tc_cfg_.variant = value == 0 ? 0 : -1;
@@ -133,6 +137,15 @@ void Engine::set_option(const std::string& name, double value) {
   } else if (name == "open_terminals") {
     if (value != 0 && value != 1) throw QFX_ERR("Option open_terminals must be 0 or 1.");
     open_terminals_ = value != 0;
+  } else if (name == "tc_debias") {
+    if (value != 0 && value != 1) throw QFX_ERR("Option tc_debias must be 0 or 1.");
+    debias_ = value != 0;
+    if (device_ >= 0) {
+      const int flag = debias_ ? 1 : 0;
+      int* p = error_flag();
+      QFX_CUDA(cudaMemcpyAsync(p + 1, &flag, sizeof(flag), cudaMemcpyHostToDevice, stream_));
+      QFX_CUDA(cudaStreamSynchronize(stream_));
+    }
   } else if (name == "exact_gates") {
     if (value != -1 && value != 0 && value != 1) throw QFX_ERR("Option exact_gates must be -1, 0 or 1.");
     exact_gates_ = int(value);
@@ -158,17 +171,19 @@ void Engine::set_option(const std::string& name, double value) {
 double Engine::get_option(const std::string& name) const {
   if (name == "tc_chunk") return tc_cfg_.chunk;
   if (name == "tc_pair") return tc_cfg_.variant == 0 ? 0 : 1;
+  if (name == "tc_variant") return tc_cfg_.variant;
   if (name == "graphs") return graphs_ ? 1 : 0;
   if (name == "max_batch") return max_batch_;
   if (name == "open_terminals") return open_terminals_ ? 1 : 0;
   if (name == "fuse_splits") return fuse_splits_ ? 1 : 0;
   if (name == "tc_wait_ns") return double(wait_ns_);
   if (name == "exact_gates") return exact_gates_;
+  if (name == "tc_debias") return debias_ ? 1 : 0;
   throw QFX_ERR("Unknown option '", name, "'.");
 }
 
 void Engine::set_tc_variant(std::size_t m, std::size_t n, std::size_t k, int variant) {
-  if (variant < -1 || variant > 2) throw QFX_ERR("Tensor-core variant must be -1, 0, 1 or 2.");
+  if (variant < -1 || variant > 3) throw QFX_ERR("Tensor-core variant must be -1, 0, 1, 2 or 3.");
   if (variant == -1)
     tc_variant_.erase({m, n, k});
   else
@@ -196,12 +211,14 @@ TcConfig Engine::tc_config(std::size_t m, std::size_t n, std::size_t k) const {
 }
 
 int* Engine::error_flag() {
-  // int[4]: the error code of the tensor-core kernels, then (bytes 8..15)
-  // the limit of their pipeline waits in ns (0: the kernels' 2 s default).
+  // The context's control block for the tensor-core kernels, int[4]: the
+  // error code they set, the truncation-bias compensation switch, then
+  // (bytes 8..15) the limit of their pipeline waits in ns (0: 2 s).
   const bool fresh = (int)bufs_.size() <= 5 || bufs_[5].bytes < 4 * sizeof(int);
   int* p = (int*)reserve(sizeof(int) * 4, 5);
   if (fresh) {
-    const unsigned long long init[2] = {0ull, wait_ns_};
+    int init[4] = {0, debias_ ? 1 : 0, 0, 0};
+    std::memcpy(init + 2, &wait_ns_, sizeof(wait_ns_));
     QFX_CUDA(cudaMemcpyAsync(p, init, sizeof(init), cudaMemcpyHostToDevice, stream_));
     QFX_CUDA(cudaStreamSynchronize(stream_));
   }

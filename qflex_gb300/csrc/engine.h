@@ -127,6 +127,7 @@ class Engine {
   bool fuse_splits_ = true;      // 3xFP16: permutes write the next product's A planes
   unsigned long long wait_ns_ = 0;  // tensor-core pipeline wait limit (0: the kernels' 2 s)
   int exact_gates_ = -1;  // gate tensors from double constants: -1 all but FP32, 0 never, 1 always
+  bool debias_ = true;    // tensor-core products compensate the truncation bias
   unsigned options_version_ = 0;  // part of the graph key: options change launches
   TcConfig tc_config(std::size_t m, std::size_t n, std::size_t k) const;
   // C = A * Bt^T on the tensor cores in the context's split precision.

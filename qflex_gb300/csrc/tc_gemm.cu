@@ -77,6 +77,12 @@ constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + STAGING_BYTES + 1024 + 256;
 constexpr int DEEP_STAGES = 5;
 constexpr int DEEP_STAGING_BYTES = EPI_WARPS * 2048;
 constexpr int DEEP_SMEM_BYTES = DEEP_STAGES * F16_STAGE_BYTES + DEEP_STAGING_BYTES + 1024 + 256;
+// The wide 3xFP16 variant: 16 epilogue warps, four per TMEM lane quadrant,
+// each draining a quarter of the tile's columns (the chunk drain is the
+// critical path when chunks are one k-step long); one 4 KB output slot per
+// warp in the same staging area. Needs the bulk-store output map.
+constexpr int WIDE_EPI_WARPS = 16;
+constexpr int WIDE_THREADS = 64 + 32 * WIDE_EPI_WARPS;
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s per wait
 
 __device__ __forceinline__ std::uint32_t smem_u32(const void* p) {
@@ -239,6 +245,24 @@ __device__ __forceinline__ void umma_f16_kstep(std::uint32_t d, std::uint32_t lo
 // scaled by powers of two).
 // BF16x3: three BF16 pieces per value (x = b0 + b1 + b2 to ~24 bits).
 enum SplitKind : int { KIND_TF32 = 0, KIND_FP16 = 1, KIND_BF16 = 2 };
+
+// Compensation of the truncation bias. The tensor core's FP32 accumulation
+// rounds toward zero, so every product comes out smaller by a fraction beta
+// of itself that depends on the split kind and on how many k-steps a TMEM
+// chunk accumulates (not on the shape). Measured on GB300 against complex128
+// products of Gaussian operands (python -m qflex_gb300.kernel_bench bias), for
+// chunks of one and two k-steps; other chunk lengths are not compensated.
+// With err[1] != 0 (option "tc_debias") every output x becomes x + beta x,
+// one fused multiply-add rounded to nearest (1 + beta itself is not a float:
+// beta is below the float spacing at 1).
+template <int KIND>
+__device__ __forceinline__ float debias_beta(const int* err, int chunk, int kblocks) {
+  if (*reinterpret_cast<const volatile int*>(err + 1) == 0) return 0.f;
+  const int c = chunk < kblocks ? chunk : kblocks;
+  if (c == 1) return KIND == KIND_FP16 ? 5.53e-8f : KIND == KIND_BF16 ? 4.47e-8f : 5.39e-8f;
+  if (c == 2) return KIND == KIND_FP16 ? 1.535e-7f : KIND == KIND_BF16 ? 2.226e-7f : 1.52e-7f;
+  return 0.f;
+}
 template <int KIND>
 __device__ __forceinline__ void umma(std::uint32_t d, std::uint64_t a, std::uint64_t b, std::uint32_t id,
                                      std::uint32_t acc) {
@@ -390,7 +414,10 @@ __device__ __forceinline__ void umma_f16_pair(std::uint32_t d_tmem, std::uint64_
 // DEEP (3xFP16 single CTA): five stages instead of four; the output leaves
 // in 2 KB boxes (32 rows x 8 complex) so that the staging area shrinks to
 // 16 KB. Needs the bulk-store output map (tma_c).
-template <int KIND, bool PAIR = false, bool DEEP = false>
+//
+// EPI (3xFP16 single CTA): epilogue warps, 8 (each drains half of the tile's
+// columns, two 4 KB output slots) or 16 (a quarter, one slot; needs tma_c).
+template <int KIND, bool PAIR = false, bool DEEP = false, int EPI = EPI_WARPS>
 __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const CUtensorMap* map_b,
                                                  const CUtensorMap* map_a2, const CUtensorMap* map_b2,
                                                  const CUtensorMap* map_c, bool tma_c,
@@ -410,6 +437,10 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
   static_assert(NST * SBYTES <= STAGE_REGION, "stages fit the shared memory of the launch");
   static_assert(!PAIR || KIND == KIND_FP16, "the CTA pair is a 3xFP16 kernel");
   static_assert(!DEEP || (KIND == KIND_FP16 && !PAIR), "the deep variant is a single-CTA 3xFP16 kernel");
+  static_assert(EPI == EPI_WARPS || (EPI == WIDE_EPI_WARPS && KIND == KIND_FP16 && !PAIR && !DEEP),
+                "16 epilogue warps: the single-CTA 3xFP16 kernel");
+  constexpr int COLS = BN * 4 / EPI;  // complex columns an epilogue warp drains and stores
+  constexpr int SLOTS = STG_BYTES / EPI / 4096;  // 4 KB output slots per epilogue warp (DEEP: unused)
   extern __shared__ __align__(1024) std::uint8_t smem_raw[];
   std::uint8_t* smem = reinterpret_cast<std::uint8_t*>((reinterpret_cast<std::uintptr_t>(smem_raw) + 1023) &
                                                        ~std::uintptr_t(1023));
@@ -464,7 +495,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], PAIR ? 2 * EPI_WARPS : EPI_WARPS);
+      mbar_init(&acc_empty[b], PAIR ? 2 * EPI : EPI);
     }
     mbar_init(mma_done, 1);
     *abort_flag = 0;
@@ -686,21 +717,22 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     // toward zero; keeping each chunk short and adding the chunks here with
     // round-to-nearest keeps the product as accurate as FP32 arithmetic.
     const int q = warp % 4;
-    const int half = (warp - 2) / 4;
+    const int part = (warp - 2) / 4;  // which COLS-wide share of the columns
     const int row = q * 32 + lane;
     float2* stg =
-        reinterpret_cast<float2*>(reinterpret_cast<std::uint8_t*>(staging) + (warp - 2) * (STG_BYTES / EPI_WARPS));
+        reinterpret_cast<float2*>(reinterpret_cast<std::uint8_t*>(staging) + (warp - 2) * (STG_BYTES / EPI));
     int c = 0;
     bool ok = true;
+    const float beta = debias_beta<KIND>(err, CHUNK, kblocks);
     // A pair's acc_empty barriers live in CTA 0.
     const std::uint32_t drained0 = PAIR ? peer_addr(&acc_empty[0], 0) : 0u;
     const std::uint32_t drained1 = PAIR ? peer_addr(&acc_empty[1], 0) : 0u;
     for (int t = first; t < total && ok; t += stride) {
       int m0, n0, batch;
       tile_of(t, m0, n0, batch);
-      float tre[BN / 2], tim[BN / 2];
+      float tre[COLS], tim[COLS];
 #pragma unroll
-      for (int j = 0; j < BN / 2; ++j) tre[j] = tim[j] = 0.f;
+      for (int j = 0; j < COLS; ++j) tre[j] = tim[j] = 0.f;
       // A's block exponent of a chunk is fetched one chunk ahead, so its
       // load latency stays out of the drain.
       const bool blocked = KIND == KIND_FP16 && a_blocks > 0 && m0 + row < m;
@@ -717,9 +749,9 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
         asm volatile("tcgen05.fence::after_thread_sync;");
         // Scale of this chunk: 1, or 2^-e of A's block for this row.
         const float sa = scale2(1.f, -e_blk);
-        const std::uint32_t base = tmem + (std::uint32_t(q * 32) << 16) + buf * 2 * BN + half * (BN / 2);
+        const std::uint32_t base = tmem + (std::uint32_t(q * 32) << 16) + buf * 2 * BN + part * COLS;
 #pragma unroll
-        for (int j0 = 0; j0 < BN / 2; j0 += 16) {
+        for (int j0 = 0; j0 < COLS; j0 += 16) {
           // 16 columns of re and of im per round trip: with the 128 running
           // sums that keeps the epilogue within its 168 registers.
           std::uint32_t vr[16], vi[16];
@@ -744,16 +776,16 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
       if (!ok) break;
       // The MMA issuer already works on the next tile. The warp's 32 x 64
       // block leaves in two 32 x 32 pieces through its staging area.
-      const int ncols = n - n0 - half * (BN / 2);
+      const int ncols = n - n0 - part * COLS;
       // 3xFP16 scale exponents: the row's (unless A's blocks were applied
       // per chunk) and, per piece, that of column j0 + lane.
       int ea = 0, eb0 = 0, eb1 = 0;
       bool fast = true;
       if (KIND == KIND_FP16) {
         ea = (a_blocks == 0 && m0 + row < m) ? exp_a[std::uint64_t(batch) * m + m0 + row] : 0;
-        const int* eb = exp_b + std::uint64_t(batch) * n + n0 + half * (BN / 2);
+        const int* eb = exp_b + std::uint64_t(batch) * n + n0 + part * COLS;
         eb0 = lane < ncols ? eb[lane] : 0;
-        eb1 = 32 + lane < ncols ? eb[32 + lane] : 0;
+        eb1 = COLS > 32 && 32 + lane < ncols ? eb[32 + lane] : eb0;
         // When every scale 2^-(ea + eb) of the warp's block is a normal
         // float, each element takes one multiply by it (exact unless the
         // result leaves the normal range, then rounded as ldexpf rounds).
@@ -767,6 +799,8 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
       // multiply is exact whenever the result is normal, and an exponent
       // beyond +-252 only arises for results far outside the float range.
       auto out = [&](float re, float im, int ebl, int j) -> float2 {
+        re = fmaf(re, beta, re);
+        im = fmaf(im, beta, im);
         if (KIND != KIND_FP16) return make_float2(re, im);
         const int ebj = __shfl_sync(0xffffffffu, ebl, j);
         if (fast) {
@@ -780,7 +814,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
       };
       float2* cb = C + std::uint64_t(batch) * c_batch_stride;
 #pragma unroll
-      for (int j0 = 0; j0 < BN / 2; j0 += 32) {
+      for (int j0 = 0; j0 < COLS; j0 += 32) {
         const int ebl = j0 ? eb1 : eb0;
         if constexpr (DEEP) {
           // Four boxes of 32 rows x 8 complex per piece, 64-byte swizzle
@@ -802,12 +836,12 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
             fence_proxy_async();
             __syncwarp();
             if (lane == 0) {
-              const int x = 2 * (n0 + half * (BN / 2) + j0 + 8 * b), y = m0 + q * 32;
+              const int x = 2 * (n0 + part * COLS + j0 + 8 * b), y = m0 + q * 32;
               if (y < m && x < 2 * n) tma_store_3d(map_c, stg, x, y, batch);
               bulk_commit();
             }
           }
-        } else if (tma_c) {
+        } else if (tma_c || EPI != EPI_WARPS) {  // the wide kernel always stores by TMA
           // Boxes of 32 rows x 16 complex in the 128-byte swizzle (16-byte
           // unit u of row r at r * 128 + ((u ^ r % 8) * 16)), stored by TMA
           // from two 4 KB slots in turn; a slot is rewritten once the box
@@ -815,8 +849,15 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
           // box, at most one other still reading).
 #pragma unroll
           for (int b = 0; b < 2; ++b) {
-            std::uint8_t* slot = reinterpret_cast<std::uint8_t*>(stg) + b * 4096;
-            if (lane == 0) bulk_wait_read1();
+            // Two slots: a box waits for the one stored two boxes earlier;
+            // one slot: for the previous box.
+            std::uint8_t* slot = reinterpret_cast<std::uint8_t*>(stg) + (b % SLOTS) * 4096;
+            if (lane == 0) {
+              if constexpr (SLOTS >= 2)
+                bulk_wait_read1();
+              else
+                bulk_wait_read();
+            }
             __syncwarp();
 #pragma unroll
             for (int jj = 0; jj < 16; jj += 2) {
@@ -830,7 +871,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
             fence_proxy_async();
             __syncwarp();
             if (lane == 0) {
-              const int x = 2 * (n0 + half * (BN / 2) + j0 + 16 * b), y = m0 + q * 32;
+              const int x = 2 * (n0 + part * COLS + j0 + 16 * b), y = m0 + q * 32;
               if (y < m && x < 2 * n) tma_store_3d(map_c, slot, x, y, batch);
               bulk_commit();
             }
@@ -846,7 +887,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
           for (int r = 0; r < 32; ++r) {
             const int gr = m0 + q * 32 + r;
             if (gr < m && j0 + lane < ncols)
-              cb[std::uint64_t(gr) * n + n0 + half * (BN / 2) + j0 + lane] = stg[r * 32 + (lane ^ r)];
+              cb[std::uint64_t(gr) * n + n0 + part * COLS + j0 + lane] = stg[r * 32 + (lane ^ r)];
           }
           __syncwarp();
         }
@@ -907,6 +948,16 @@ __global__ void __launch_bounds__(THREADS, 1)
 }
 
 // The 3xFP16 product on CTA pairs (see cgemm_split_body).
+__global__ void __launch_bounds__(WIDE_THREADS, 1)
+    cgemm_fp16x3_wide_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                             const __grid_constant__ CUtensorMap map_c, float2* __restrict__ C, int m, int n, int k,
+                             int batches, std::uint64_t c_batch_stride, int* __restrict__ err, int CHUNK,
+                             const int* __restrict__ exp_a, const int* __restrict__ exp_b, int a_blocks) {
+  cgemm_split_body<KIND_FP16, false, false, WIDE_EPI_WARPS>(&map_a, &map_b, nullptr, nullptr, &map_c, true, C, m,
+                                                           n, k, batches, c_batch_stride, err, CHUNK, exp_a, exp_b,
+                                                           a_blocks);
+}
+
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
     cgemm_fp16x3_pair_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                              const __grid_constant__ CUtensorMap map_c, int tma_c, float2* __restrict__ C, int m,
@@ -1423,11 +1474,12 @@ unsigned persistent_grid(std::size_t tiles) {
 TcConfig tc_default_config() {
   TcConfig c;
   // k-steps per TMEM chunk. The tensor core's FP32 accumulation truncates,
-  // which shrinks every product by a few 1e-8 per truncating add; a chunk's
-  // adds are the unit of that bias. Measured on 256 amplitudes of the 16-slice
-  // 7x7 (1+32+1) workload against the FP64 oracle (3xFP16): chunk 2 shrinks
-  // every amplitude by 4.9e-6 (largest error 1.1e-5 of the RMS amplitude),
-  // chunk 1 by 2.2e-6 (5.6e-6) at 7 % less throughput.
+  // which shrinks every product by a fraction that grows with the chunk
+  // (debias_beta). Measured on 256 amplitudes of the 16-slice 7x7 (1+32+1)
+  // workload against the FP64 oracle (3xFP16): chunk 2 without compensation
+  // shrinks every amplitude by 4.9e-6 (largest error 1.2e-5 of the RMS
+  // amplitude), chunk 1 by 2.3e-6 (5.8e-6) at 7 % less throughput, chunk 2
+  // with the compensation (the default) by 1e-7 (2.6e-6).
   if (const char* e = std::getenv("QFLEX_TC_CHUNK")) {
     const int v = std::atoi(e);
     if (v >= 1 && v <= 64) c.chunk = v;
@@ -1518,6 +1570,8 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
     check(cudaFuncSetAttribute(cgemm_fp16x3_deep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                DEEP_SMEM_BYTES),
           "cudaFuncSetAttribute");
+    check(cudaFuncSetAttribute(cgemm_fp16x3_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
+          "cudaFuncSetAttribute");
   });
   const bool use_pair = cfg.variant == 1 || (cfg.variant < 0 && m >= 2 * BM);
   const std::size_t kpad = (k + 15) / 16 * 16;
@@ -1580,6 +1634,12 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
     cgemm_fp16x3_deep_kernel<<<grid, THREADS, DEEP_SMEM_BYTES, s>>>(
         ma_rows, mb, mcn, 1, C, (int)m, (int)n, (int)k, batch, batch_stride, err, cfg.chunk, ea, eb, a_blocks);
     check(cudaGetLastError(), "cgemm_fp16x3_deep");
+    return;
+  }
+  if (cfg.variant == 3 && tma_c) {
+    cgemm_fp16x3_wide_kernel<<<grid, WIDE_THREADS, SMEM_BYTES, s>>>(
+        ma_rows, mb, mc, C, (int)m, (int)n, (int)k, batch, batch_stride, err, cfg.chunk, ea, eb, a_blocks);
+    check(cudaGetLastError(), "cgemm_fp16x3_wide");
     return;
   }
   cgemm_fp16x3_kernel<<<grid, THREADS, SMEM_BYTES, s>>>(ma_rows, mb, mc, tma_c, C, (int)m, (int)n, (int)k, batch,

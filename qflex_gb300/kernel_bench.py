@@ -3,6 +3,7 @@
     python -m qflex_gb300.kernel_bench gemm --m 4096 --n 4096 --k 4096 --precision tf32x3
     python -m qflex_gb300.kernel_bench gemm --m 65536 --n 256 --k 256 --precision fp16x3 --batch 8
     python -m qflex_gb300.kernel_bench permute --bits 24 --seed 1
+    python -m qflex_gb300.kernel_bench step --steps 3 --warmup 2 [--ordering supplied] [--chunk 2]
 
 Times launches with CUDA events on the context's stream (after warm-up) and
 prints one JSON line: average milliseconds per launch and the achieved
@@ -42,20 +43,22 @@ def _time(torch, stream, fn, reps: int, warmup: int) -> float:
 
 
 def gemm(m: int, n: int, k: int, precision: str, reps: int, warmup: int, batch: int = 1,
-         variant: int = -1) -> dict:
+         variant: int = -1, chunk: int = 0) -> dict:
     """`batch` products per launch (operands of entry b at b * (m k + k n +
     m n) complex); `variant` >= 0 sets the tensor-core kernel variant of the
     shape (qflex_gb300_set_tc_variant)."""
     torch, ctx, stream = _setup(precision)
     if variant >= 0:
         ctx.set_tc_variant(m, n, k, variant)
+    if chunk > 0:
+        ctx.set_option("tc_chunk", chunk)
     stride = m * k + k * n + m * n
     buf = torch.randn((batch, stride), dtype=torch.complex64, device="cuda")
     base = buf.data_ptr()
     a, b, c = base, base + 8 * m * k, base + 8 * (m * k + k * n)
     ms = _time(torch, stream, lambda: ctx.multiply(a, b, c, m, n, k, batch, stride), reps, warmup)
     return {"kernel": "multiply", "precision": precision, "m": m, "n": n, "k": k, "batch": batch,
-            "variant": variant, "ms": ms, "tflops": 8.0 * m * n * k * batch / (ms / 1e3) / 1e12}
+            "variant": variant, "debias": debias, "chunk": chunk, "ms": ms, "tflops": 8.0 * m * n * k * batch / (ms / 1e3) / 1e12}
 
 
 def permute(bits: int, seed: int, reps: int, warmup: int) -> dict:
@@ -68,6 +71,63 @@ def permute(bits: int, seed: int, reps: int, warmup: int) -> dict:
                lambda: ctx.permute(src.data_ptr(), dst.data_ptr(), [2] * bits, order), reps, warmup)
     return {"kernel": "permute", "bits": bits, "order": order, "ms": ms,
             "gbs": 16.0 * (1 << bits) / (ms / 1e3) / 1e9}
+
+
+def step(precision: str, steps: int, warmup: int, batch: int, ordering: str, chunk: int, max_batch: int,
+         variant: int = -1, debias: int = -1) -> dict:
+    """The benchmark step alone: evaluate_many over `batch` new output
+    strings of the 7x7 (1+32+1) workload (16 cut slices), `warmup` untimed
+    steps then `steps` timed ones (device time), with the learned or the
+    supplied ordering."""
+    torch, ctx, stream = _setup(precision)
+    from . import rqc
+    circuit, supplied, grid, initial, finals = rqc.workload("c3")
+    text = rqc.ordering_7x7_learned() if ordering == "learned" else supplied
+    if chunk > 0:
+        ctx.set_option("tc_chunk", chunk)
+    if max_batch > 0:
+        ctx.set_option("max_batch", max_batch)
+    if variant >= 0:
+        ctx.set_option("tc_variant", variant)
+    if debias >= 0:
+        ctx.set_option("tc_debias", debias)
+    for w in range(warmup):
+        ctx.evaluate_many(circuit, text, grid, initial, finals[batch * w:batch * (w + 1)], 1 << 40)
+    ms = 0.0
+    for s in range(steps):
+        lo = batch * (warmup + s)
+        ctx.evaluate_many(circuit, text, grid, initial, finals[lo:lo + batch], 1 << 40)
+        ms += ctx.stats()["device_ms"]
+    return {"kernel": "step", "precision": precision, "ordering": ordering, "chunk": chunk, "max_batch": max_batch,
+            "variant": variant, "debias": debias,
+            "strings": steps * batch, "ms_per_step": ms / steps,
+            "amplitudes_per_s": steps * batch / (ms / 1e3)}
+
+
+def bias(precision: str, chunk: int, debias: int, shapes) -> dict:
+    """Mean relative bias of split tensor-core products against complex128
+    products of the same complex64 operands (Gaussian entries): beta =
+    Re<C - C64, C64> / <C64, C64>, the fraction of itself a product loses to
+    the tensor core's truncating accumulation, and the relative RMS error.
+    The constants of tc_debias come from this measurement."""
+    torch, ctx, stream = _setup(precision)
+    ctx.set_option("tc_chunk", chunk)
+    ctx.set_option("tc_debias", debias)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    rows = []
+    for m, n, k in shapes:
+        A = torch.randn((m, k), dtype=torch.complex64, device="cuda", generator=g)
+        B = torch.randn((k, n), dtype=torch.complex64, device="cuda", generator=g)
+        C = torch.empty((m, n), dtype=torch.complex64, device="cuda")
+        torch.cuda.synchronize()
+        ctx.multiply(A.data_ptr(), B.data_ptr(), C.data_ptr(), m, n, k)
+        ctx.synchronize()
+        ref = A.to(torch.complex128) @ B.to(torch.complex128)
+        d = C.to(torch.complex128) - ref
+        norm = float((ref.abs() ** 2).sum())
+        rows.append({"m": m, "n": n, "k": k, "beta": float((d * ref.conj()).real.sum()) / norm,
+                     "rel_rms": (float((d.abs() ** 2).sum()) / norm) ** 0.5})
+    return {"kernel": "bias", "precision": precision, "chunk": chunk, "debias": debias, "shapes": rows}
 
 
 def main() -> None:
@@ -84,12 +144,32 @@ def main() -> None:
     q = sub.add_parser("permute")
     q.add_argument("--bits", type=int, default=24)
     q.add_argument("--seed", type=int, default=1)
+    bs = sub.add_parser("bias")
+    bs.add_argument("--precision", default="fp16x3")
+    bs.add_argument("--chunk", type=int, default=1)
+    bs.add_argument("--debias", type=int, default=0)
+    st = sub.add_parser("step")
+    st.add_argument("--precision", default="fp16x3")
+    st.add_argument("--steps", type=int, default=3)
+    st.add_argument("--batch", type=int, default=8)
+    st.add_argument("--ordering", default="learned", choices=["learned", "supplied"])
+    st.add_argument("--chunk", type=int, default=0, help="TMEM chunk (0: the default)")
+    st.add_argument("--max-batch", type=int, default=4, help="strings per device pass (0: all that fit)")
+    st.add_argument("--variant", type=int, default=-1, help="tensor-core kernel of every product (tc_variant)")
+    st.add_argument("--debias", type=int, default=-1, help="tc_debias option (-1: the default)")
     for s in (g, q):
         s.add_argument("--reps", type=int, default=5)
+    for s in (g, q, st):
         s.add_argument("--warmup", type=int, default=2)
+    g.add_argument("--chunk", type=int, default=0, help="TMEM chunk (0: the default)")
     a = p.parse_args()
     if a.what == "gemm":
-        out = gemm(a.m, a.n, a.k, a.precision, a.reps, a.warmup, a.batch, a.variant)
+        out = gemm(a.m, a.n, a.k, a.precision, a.reps, a.warmup, a.batch, a.variant, a.chunk)
+    elif a.what == "step":
+        out = step(a.precision, a.steps, a.warmup, a.batch, a.ordering, a.chunk, a.max_batch, a.variant, a.debias)
+    elif a.what == "bias":
+        out = bias(a.precision, a.chunk, a.debias,
+                   [(4096, 4096, 4096), (65536, 256, 256), (4096, 256, 4096), (16384, 1024, 64), (1024, 1024, 16)])
     else:
         out = permute(a.bits, a.seed, a.reps, a.warmup)
     print(json.dumps(out))
