@@ -58,7 +58,7 @@ def gemm(m: int, n: int, k: int, precision: str, reps: int, warmup: int, batch: 
     a, b, c = base, base + 8 * m * k, base + 8 * (m * k + k * n)
     ms = _time(torch, stream, lambda: ctx.multiply(a, b, c, m, n, k, batch, stride), reps, warmup)
     return {"kernel": "multiply", "precision": precision, "m": m, "n": n, "k": k, "batch": batch,
-            "variant": variant, "debias": debias, "chunk": chunk, "ms": ms, "tflops": 8.0 * m * n * k * batch / (ms / 1e3) / 1e12}
+            "variant": variant, "chunk": chunk, "ms": ms, "tflops": 8.0 * m * n * k * batch / (ms / 1e3) / 1e12}
 
 
 def permute(bits: int, seed: int, reps: int, warmup: int) -> dict:
