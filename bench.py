@@ -37,11 +37,11 @@ METRIC = "amplitudes/s on 7x7 1+32+1 RQC; split-precision vs FP32, rel err≤1e-
 UNIT = "amplitudes/s"
 WORKLOAD = "c3"
 FP32_PEAK_NOMINAL = 152 * 128 * 2 * 2.07e9 / 1e12  # TFLOP/s, FP32 CUDA-core FMA
-# DRAM bytes (read + write) of one launch of the dominant product, from ncu
-# captures summarised in profiles/.
-# ncu dram__bytes_read.sum + dram__bytes_write.sum of one product kernel
-# launch of this shape with batch 1 (profiles/tc_*_4096.md).
-TRAFFIC = {("tf32x3", 4096, 4096, 4096): 2.322e9, ("fp16x3", 4096, 4096, 4096): 1.270e9}
+# DRAM bytes (read + write) per product of the dominant shape, from the ncu
+# captures summarised in profiles/ (dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch divided by its products): 3xTF32 at 1
+# product per launch, 3xFP16 at 4 (the step's pass size), 5.728 GB / 4.
+TRAFFIC = {("tf32x3", 4096, 4096, 4096): 2.322e9, ("fp16x3", 4096, 4096, 4096): 1.432e9}
 
 
 def parse():
@@ -528,8 +528,8 @@ def main():
                          "unit": "TFLOP/s algorithmic"},
                 "traffic": (TRAFFIC[(args.precision, m, n, k)] * pbatch
                             if (args.precision, m, n, k) in TRAFFIC else None),
-                "traffic_source": "ncu dram__bytes_read+write of one batch-1 launch of this shape (profiles/), "
-                                  "times the batch: each product of the batch reads its own operands",
+                "traffic_source": "ncu dram__bytes_read+write per product of this shape (profiles/tc_*_4096.md), "
+                                  "times the products per launch",
                 "algorithmic_bytes": 8.0 * (m * k + k * n + m * n) * pbatch,
                 "timing": f"CUDA events around each of the {launches} launches of this shape (batch {pbatch}) "
                           f"in one profiled pass of the step on the context stream; {100 * share:.0f}% of the pass",
