@@ -132,7 +132,7 @@ size_t qflex_gb300_last_ops(const qflex_gb300_context* ctx, double* out, size_t 
  *                (cta_group::2, 256 x 128 tile) kernel; 0: every product uses
  *                the single-CTA 128 x 128 tile (default 0, or QFLEX_TC_PAIR)
  *   "tc_variant" tensor-core kernel of every product without a per-shape
- *                choice (qflex_gb300_set_tc_variant): 0..3 as listed there
+ *                choice (qflex_gb300_set_tc_variant): 0..4 as listed there
  *                (default 0; "tc_pair" sets 0 or the pair-for-m >= 256 rule)
  *   "graphs"     1: capture a repeated device pass in a CUDA graph and
  *                replay it (default 1, or QFLEX_GB300_GRAPHS)
@@ -171,7 +171,8 @@ int qflex_gb300_get_option(const qflex_gb300_context* ctx, const char* name, dou
 /* Tensor-core kernel for products of shape (m, n, k), e.g. chosen by an
  * autotuner: 0 single CTA, 1 CTA pair (needs m >= 64), 2 single CTA with a
  * deeper operand pipeline (3xFP16), 3 single CTA with 16 epilogue warps
- * (3xFP16; outputs that cannot take bulk tensor stores use 0); the other
+ * (3xFP16; outputs that cannot take bulk tensor stores use 0), 4 single CTA
+ * with 64-column tiles and four TMEM chunk buffers (3xFP16); the other
  * precisions take 0. -1 removes the override. Overrides "tc_pair" for that
  * shape. */
 int qflex_gb300_set_tc_variant(qflex_gb300_context* ctx, size_t m, size_t n, size_t k, int variant);

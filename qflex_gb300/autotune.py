@@ -21,7 +21,7 @@ from typing import Dict, List, Optional, Sequence, Tuple
 from ._lib import FP16X3, TF32X3, Context
 
 VARIANTS = (0, 1)  # single CTA, CTA pair
-FP16_VARIANTS = (0, 1, 2, 3)  # + the five-stage and the 16-epilogue-warp 3xFP16 kernels
+FP16_VARIANTS = (0, 1, 2, 3, 4)  # + five stages, 16 epilogue warps, 64-column tiles (3xFP16)
 
 
 def variants(ctx: Context) -> Tuple[int, ...]:

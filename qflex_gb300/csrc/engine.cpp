@@ -122,8 +122,8 @@ void Engine::set_option(const std::string& name, double value) {
       throw QFX_ERR("Option tc_chunk must be an integer in 1..64.");
     tc_cfg_.chunk = int(value);
   } else if (name == "tc_variant") {
-    if (!(value >= 0 && value <= 3) || value != double(int(value)))
-      throw QFX_ERR("Option tc_variant must be 0, 1, 2 or 3.");
+    if (!(value >= 0 && value <= 4) || value != double(int(value)))
+      throw QFX_ERR("Option tc_variant must be 0, 1, 2, 3 or 4.");
     tc_cfg_.variant = int(value);
   } else if (name == "tc_pair") {
     if (value != 0 && value != 1) throw QFX_ERR("Option tc_pair must be 0 or 1.");
@@ -183,7 +183,7 @@ double Engine::get_option(const std::string& name) const {
 }
 
 void Engine::set_tc_variant(std::size_t m, std::size_t n, std::size_t k, int variant) {
-  if (variant < -1 || variant > 3) throw QFX_ERR("Tensor-core variant must be -1, 0, 1, 2 or 3.");
+  if (variant < -1 || variant > 4) throw QFX_ERR("Tensor-core variant must be -1, 0, 1, 2, 3 or 4.");
   if (variant == -1)
     tc_variant_.erase({m, n, k});
   else

@@ -222,13 +222,16 @@ __device__ __forceinline__ void umma_f16(std::uint32_t d_tmem, std::uint64_t a, 
 // 16-byte units: A re lo +2, A im hi +4, lo +6; B -im +1024, +1026, B re
 // +1536, +1538. `acc` = 0 starts the accumulator.
 __device__ __forceinline__ void umma_f16_kstep(std::uint32_t d, std::uint32_t lo, std::uint32_t hia,
-                                               std::uint32_t hib, std::uint32_t idesc, std::uint32_t acc) {
+                                               std::uint32_t hib, std::uint32_t idesc, std::uint32_t acc,
+                                               std::uint32_t bstep = 512) {
+  // bstep: distance from the -Bi block to the Br block in 16-byte units
+  // (rows of the tile x 64 bytes / 16).
   asm volatile(
       "{\n .reg .pred p0, p1;\n .reg .b32 l1, l2, l3, l4, l5, l6, l7;\n"
       " .reg .b64 arh, arl, aih, ail, b2h, b2l, b1h, b1l;\n"
       " setp.ne.b32 p0, %5, 0;\n setp.eq.b32 p1, %5, %5;\n"
       " add.u32 l1, %1, 2;\n add.u32 l2, %1, 4;\n add.u32 l3, %1, 6;\n add.u32 l4, %1, 1024;\n"
-      " add.u32 l5, %1, 1026;\n add.u32 l6, %1, 1536;\n add.u32 l7, %1, 1538;\n"
+      " add.u32 l5, %1, 1026;\n add.u32 l6, l4, %6;\n add.u32 l7, l6, 2;\n"
       " mov.b64 arh, {%1, %2};\n mov.b64 arl, {l1, %2};\n mov.b64 aih, {l2, %2};\n mov.b64 ail, {l3, %2};\n"
       " mov.b64 b2h, {l4, %3};\n mov.b64 b2l, {l5, %3};\n mov.b64 b1h, {l6, %3};\n mov.b64 b1l, {l7, %3};\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], arh, b1l, %4, p0;\n"
@@ -237,7 +240,7 @@ __device__ __forceinline__ void umma_f16_kstep(std::uint32_t d, std::uint32_t lo
       " tcgen05.mma.cta_group::1.kind::f16 [%0], ail, b2h, %4, p1;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], arh, b1h, %4, p1;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], aih, b2h, %4, p1;\n}\n" ::"r"(d),
-      "r"(lo), "r"(hia), "r"(hib), "r"(idesc), "r"(acc));
+      "r"(lo), "r"(hia), "r"(hib), "r"(idesc), "r"(acc), "r"(bstep));
 }
 
 // Operand kinds of the single-CTA kernel: 3xTF32 planes (8 values of 4
@@ -417,7 +420,12 @@ __device__ __forceinline__ void umma_f16_pair(std::uint32_t d_tmem, std::uint64_
 //
 // EPI (3xFP16 single CTA): epilogue warps, 8 (each drains half of the tile's
 // columns, two 4 KB output slots) or 16 (a quarter, one slot; needs tma_c).
-template <int KIND, bool PAIR = false, bool DEEP = false, int EPI = EPI_WARPS>
+//
+// TBN (3xFP16 single CTA): complex columns of a tile, 128 or 64. With 64 the
+// MMAs are N = 128, a stage is 28 KB (five of them), and TMEM holds four
+// chunk buffers instead of two, so the MMAs can run three chunks ahead of an
+// epilogue that is storing a tile (products with a short k).
+template <int KIND, bool PAIR = false, bool DEEP = false, int EPI = EPI_WARPS, int TBN = BN>
 __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const CUtensorMap* map_b,
                                                  const CUtensorMap* map_a2, const CUtensorMap* map_b2,
                                                  const CUtensorMap* map_c, bool tma_c,
@@ -427,10 +435,16 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
                                                  const int* __restrict__ exp_b, int a_blocks) {
   constexpr int KSTEP = KIND == KIND_TF32 ? 8 : 16;  // k values per plane row of 32 bytes
   constexpr int TAIL = BM * 64;                       // BF16 third-piece tile of one operand
-  constexpr int NST = KIND == KIND_BF16 ? 3 : (KIND == KIND_FP16 ? (PAIR || DEEP ? 5 : 4) : STAGES);
+  constexpr bool NARROW = TBN != BN;
+  constexpr int NST = KIND == KIND_BF16 ? 3 : (KIND == KIND_FP16 ? (PAIR || DEEP || NARROW ? 5 : 4) : STAGES);
+  constexpr int F16_BBLOCK = TBN * 64;  // one B block: TBN rows of 64 bytes
   constexpr int SBYTES = KIND == KIND_BF16   ? 2 * (TILE_A + TAIL)
-                         : KIND == KIND_FP16 ? (PAIR ? 4 * F16_BLOCK : F16_STAGE_BYTES)
+                         : KIND == KIND_FP16 ? (PAIR ? 4 * F16_BLOCK : 2 * F16_BLOCK + 3 * F16_BBLOCK)
                                              : STAGE_BYTES;
+  constexpr int NBUF = TMEM_COLS / (2 * TBN);  // TMEM chunk buffers of (re, im)
+  static_assert(!NARROW || (TBN == 64 && KIND == KIND_FP16 && !PAIR && !DEEP && EPI == EPI_WARPS),
+                "the narrow tile is a single-CTA 3xFP16 kernel");
+  static_assert(SBYTES % 1024 == 0, "stages keep the 1024-byte alignment of the 128-byte swizzle");
   constexpr int TM = PAIR ? 2 * BM : BM;  // rows of a tile
   constexpr int STAGE_REGION = DEEP ? DEEP_STAGES * F16_STAGE_BYTES : STAGES * STAGE_BYTES;
   constexpr int STG_BYTES = DEEP ? DEEP_STAGING_BYTES : STAGING_BYTES;
@@ -439,7 +453,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
   static_assert(!DEEP || (KIND == KIND_FP16 && !PAIR), "the deep variant is a single-CTA 3xFP16 kernel");
   static_assert(EPI == EPI_WARPS || (EPI == WIDE_EPI_WARPS && KIND == KIND_FP16 && !PAIR && !DEEP),
                 "16 epilogue warps: the single-CTA 3xFP16 kernel");
-  constexpr int COLS = BN * 4 / EPI;  // complex columns an epilogue warp drains and stores
+  constexpr int COLS = TBN * 4 / EPI;  // complex columns an epilogue warp drains and stores
   constexpr int SLOTS = STG_BYTES / EPI / 4096;  // 4 KB output slots per epilogue warp (DEEP: unused)
   extern __shared__ __align__(1024) std::uint8_t smem_raw[];
   std::uint8_t* smem = reinterpret_cast<std::uint8_t*>((reinterpret_cast<std::uintptr_t>(smem_raw) + 1023) &
@@ -448,9 +462,9 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
   float2* staging = reinterpret_cast<float2*>(smem + STAGE_REGION);
   std::uint64_t* full = reinterpret_cast<std::uint64_t*>(smem + STAGE_REGION + STG_BYTES);
   std::uint64_t* empty = full + NST;
-  std::uint64_t* acc_full = empty + NST;    // [2]: a chunk accumulator is complete
-  std::uint64_t* acc_empty = acc_full + 2;  // [2]: a chunk accumulator was drained
-  std::uint64_t* mma_done = acc_empty + 2;  // every issued MMA has completed
+  std::uint64_t* acc_full = empty + NST;       // [NBUF]: a chunk accumulator is complete
+  std::uint64_t* acc_empty = acc_full + NBUF;  // [NBUF]: a chunk accumulator was drained
+  std::uint64_t* mma_done = acc_empty + NBUF;  // every issued MMA has completed
   std::uint32_t* tmem_slot = reinterpret_cast<std::uint32_t*>(mma_done + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
@@ -460,7 +474,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
   const int first = PAIR ? blockIdx.x / 2 : blockIdx.x;
   const int stride = PAIR ? gridDim.x / 2 : gridDim.x;
   const int tiles_m = (m + TM - 1) / TM;
-  const int tiles_n = (n + BN - 1) / BN;
+  const int tiles_n = (n + TBN - 1) / TBN;
   const int per_batch = tiles_m * tiles_n;
   const int total = per_batch * batches;
   // Tiles run in groups of 8 row-tiles so that the CTAs working at one time
@@ -472,7 +486,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     const int group = r / per_group, in_group = r % per_group;
     const int group_m = min(8, tiles_m - group * 8);
     m0 = (group * 8 + in_group % group_m) * TM + int(rank) * BM;
-    n0 = (in_group / group_m) * BN;
+    n0 = (in_group / group_m) * TBN;
   };
   // Waits on barriers that the other CTA of a pair (or its MMA commits) may
   // complete use cluster scope.
@@ -493,7 +507,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < NBUF; ++b) {
       mbar_init(&acc_full[b], 1);
       mbar_init(&acc_empty[b], PAIR ? 2 * EPI : EPI);
     }
@@ -544,8 +558,8 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
             // (-im), 0 (re) and 32 (im), hi and lo each.
             tma_load_4d(map_a, &full[s], st, 0, m0, kb, batch);
             tma_load_4d(map_b, &full[s], st + 2 * F16_BLOCK, 64, n0, kb, batch);
-            tma_load_4d(map_b, &full[s], st + 3 * F16_BLOCK, 0, n0, kb, batch);
-            tma_load_4d(map_b, &full[s], st + 4 * F16_BLOCK, 32, n0, kb, batch);
+            tma_load_4d(map_b, &full[s], st + 2 * F16_BLOCK + F16_BBLOCK, 0, n0, kb, batch);
+            tma_load_4d(map_b, &full[s], st + 2 * F16_BLOCK + 2 * F16_BBLOCK, 32, n0, kb, batch);
           } else {
             tma_load_4d(map_a, &full[s], st, 0, m0, kb, batch);
             tma_load_4d(map_b, &full[s], st + TILE_A, 0, n0, kb, batch);
@@ -577,7 +591,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     // Chunk c (CHUNK k-steps of one tile; c counts across tiles) accumulates
     // from zero into TMEM buffer c % 2; the epilogue warps add it into their
     // FP32 registers and free it.
-    const std::uint32_t idp = idesc_kind<KIND>(BM, BN, false), idn = idesc_kind<KIND>(BM, BN, true);
+    const std::uint32_t idp = idesc_kind<KIND>(BM, TBN, false), idn = idesc_kind<KIND>(BM, TBN, true);
     // 3xFP16: descriptor of stage 0's A re hi plane; the stage's others
     // follow at fixed offsets (umma_f16_kstep), stage s at + s SBYTES / 16.
     const std::uint64_t f16d0 = smem_desc_sw128(smem_u32(smem));
@@ -592,12 +606,12 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     for (int t = first; t < total && go; t += stride) {
       kc = 0;
       for (int kb = 0; kb < kblocks; ++kb) {
-        const int buf = c & 1;
+        const int buf = c % NBUF;
         const bool first = kc == 0;
-        if (first && c >= 2) {
+        if (first && c >= NBUF) {
           // The epilogue's TMEM reads of this buffer precede the MMAs that
           // overwrite it.
-          if (!wait(&acc_empty[buf], ((c >> 1) - 1) & 1, 4)) {
+          if (!wait(&acc_empty[buf], ((c / NBUF) - 1) & 1, 4)) {
             go = false;
             break;
           }
@@ -609,7 +623,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
           go = false;
           break;
         }
-        const std::uint32_t d_re = tmem + buf * 2 * BN, d_im = d_re + BN;
+        const std::uint32_t d_re = tmem + buf * 2 * TBN, d_im = d_re + TBN;
         const std::uint32_t a0 = smem_u32(smem + s * SBYTES);
         const std::uint32_t acc = first ? 0u : 1u;
         if constexpr (PAIR) {
@@ -636,7 +650,7 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
           // Stage s's descriptors: stage 0's with the start address moved
           // by s * SBYTES (the 14-bit field cannot carry: shared memory is
           // below 256 KB).
-          umma_f16_kstep(d_re, f16_lo, f16_hia, f16_hib, idesc_f16(BM, 2 * BN, false), acc);
+          umma_f16_kstep(d_re, f16_lo, f16_hia, f16_hib, idesc_f16(BM, 2 * TBN, false), acc, F16_BBLOCK / 16);
           (void)d_im;
         } else {
           const std::uint32_t b0 = a0 + TILE_A;
@@ -739,24 +753,24 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
       const int* eblk = blocked ? exp_a + (std::uint64_t(batch) * m + m0 + row) * a_blocks : nullptr;
       int e_next = blocked ? eblk[0] : 0;
       for (int cc = 0; cc < chunks; ++cc, ++c) {
-        const int buf = c & 1;
+        const int buf = c % NBUF;
         const int e_blk = e_next;
         if (blocked && cc + 1 < chunks) e_next = eblk[((cc + 1) * CHUNK * KSTEP) / 32];
-        if (!wait(&acc_full[buf], (c >> 1) & 1, 3)) {
+        if (!wait(&acc_full[buf], (c / NBUF) & 1, 3)) {
           ok = false;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
         // Scale of this chunk: 1, or 2^-e of A's block for this row.
         const float sa = scale2(1.f, -e_blk);
-        const std::uint32_t base = tmem + (std::uint32_t(q * 32) << 16) + buf * 2 * BN + part * COLS;
+        const std::uint32_t base = tmem + (std::uint32_t(q * 32) << 16) + buf * 2 * TBN + part * COLS;
 #pragma unroll
         for (int j0 = 0; j0 < COLS; j0 += 16) {
           // 16 columns of re and of im per round trip: with the 128 running
           // sums that keeps the epilogue within its 168 registers.
           std::uint32_t vr[16], vi[16];
           TMEM_LD16(base + j0, vr);
-          TMEM_LD16(base + BN + j0, vi);
+          TMEM_LD16(base + TBN + j0, vi);
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
@@ -956,6 +970,16 @@ __global__ void __launch_bounds__(WIDE_THREADS, 1)
   cgemm_split_body<KIND_FP16, false, false, WIDE_EPI_WARPS>(&map_a, &map_b, nullptr, nullptr, &map_c, true, C, m,
                                                            n, k, batches, c_batch_stride, err, CHUNK, exp_a, exp_b,
                                                            a_blocks);
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    cgemm_fp16x3_narrow_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                               const __grid_constant__ CUtensorMap map_c, int tma_c, float2* __restrict__ C, int m,
+                               int n, int k, int batches, std::uint64_t c_batch_stride, int* __restrict__ err,
+                               int CHUNK, const int* __restrict__ exp_a, const int* __restrict__ exp_b, int a_blocks) {
+  cgemm_split_body<KIND_FP16, false, false, EPI_WARPS, 64>(&map_a, &map_b, nullptr, nullptr, &map_c, tma_c != 0, C, m,
+                                                          n, k, batches, c_batch_stride, err, CHUNK, exp_a, exp_b,
+                                                          a_blocks);
 }
 
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
@@ -1572,6 +1596,8 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
           "cudaFuncSetAttribute");
     check(cudaFuncSetAttribute(cgemm_fp16x3_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
           "cudaFuncSetAttribute");
+    check(cudaFuncSetAttribute(cgemm_fp16x3_narrow_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES),
+          "cudaFuncSetAttribute");
   });
   const bool use_pair = cfg.variant == 1 || (cfg.variant < 0 && m >= 2 * BM);
   const std::size_t kpad = (k + 15) / 16 * 16;
@@ -1634,6 +1660,16 @@ void launch_cgemm_fp16x3(const float2* A, const float2* Bt, float2* C, std::size
     cgemm_fp16x3_deep_kernel<<<grid, THREADS, DEEP_SMEM_BYTES, s>>>(
         ma_rows, mb, mcn, 1, C, (int)m, (int)n, (int)k, batch, batch_stride, err, cfg.chunk, ea, eb, a_blocks);
     check(cudaGetLastError(), "cgemm_fp16x3_deep");
+    return;
+  }
+  if (cfg.variant == 4) {
+    // 64-column tiles: B boxes of 64 rows.
+    const CUtensorMap mb64 = plane_map_f16(pb, n, kpad, batch, 64, 96);
+    const std::size_t tiles64 = ((m + BM - 1) / BM) * ((n + 63) / 64);
+    dim3 grid64(persistent_grid(tiles64 * (std::size_t)batch), 1, 1);
+    cgemm_fp16x3_narrow_kernel<<<grid64, THREADS, SMEM_BYTES, s>>>(ma_rows, mb64, mc, tma_c, C, (int)m, (int)n, (int)k,
+                                                                  batch, batch_stride, err, cfg.chunk, ea, eb, a_blocks);
+    check(cudaGetLastError(), "cgemm_fp16x3_narrow");
     return;
   }
   if (cfg.variant == 3 && tma_c) {

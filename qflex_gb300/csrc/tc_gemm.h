@@ -19,7 +19,8 @@ struct TcConfig {
   int chunk = 2;     // k-steps per TMEM accumulation chunk, 1..64 (QFLEX_TC_CHUNK)
   int variant = 0;   // 0: single CTA; 1: CTA pair; -1: CTA pair when m >= 256, else single;
                      // 2: 3xFP16 single CTA with five stages; 3: 3xFP16 single CTA with 16
-                     // epilogue warps (others: single CTA)
+                     // epilogue warps; 4: 3xFP16 single CTA with 64-column tiles and four
+                     // TMEM chunk buffers (others: single CTA)
 };
 // Defaults: chunk from QFLEX_TC_CHUNK, variant -1 when QFLEX_TC_PAIR=1, 2 when
 // QFLEX_TC_DEEP=1.

@@ -26,12 +26,14 @@ def test_options_round_trip_and_validation(built_lib):
     c.set_tc_variant(4096, 4096, 4096, 2)
     c.set_tc_variant(4096, 4096, 4096, 3)
     c.set_tc_variant(4096, 4096, 4096, -1)
+    c.set_tc_variant(4096, 4096, 4096, 4)
+    c.set_tc_variant(4096, 4096, 4096, -1)
     with pytest.raises(QflexGb300Error):
-        c.set_tc_variant(64, 64, 64, 4)
-    c.set_option("tc_variant", 3)
-    assert c.get_option("tc_variant") == 3
+        c.set_tc_variant(64, 64, 64, 5)
+    c.set_option("tc_variant", 4)
+    assert c.get_option("tc_variant") == 4
     with pytest.raises(QflexGb300Error):
-        c.set_option("tc_variant", 4)
+        c.set_option("tc_variant", 5)
 
 
 def test_tc_shapes_of_7x7_plan(built_lib):
@@ -113,9 +115,9 @@ def test_fused_fp16_planes_match_split(built_lib):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("variant", [1, 2, 3], ids=["pair", "deep", "wide"])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4], ids=["pair", "deep", "wide", "narrow"])
 def test_fp16x3_variant_matches_single_and_fp64(built_lib, variant):
-    """The CTA-pair, five-stage and 16-epilogue-warp 3xFP16 kernels on every product of one
+    """The CTA-pair, five-stage, 16-epilogue-warp and 64-column 3xFP16 kernels on every product of one
     7x7 slice (fused plane permutations included) against the single-CTA
     kernel and the FP64 oracle."""
     from oracle import qflex_oracle as qo
@@ -138,8 +140,8 @@ def test_fp16x3_variant_matches_single_and_fp64(built_lib, variant):
 def test_variant_sets_per_precision(built_lib):
     """The product tuner times the five-stage kernel only for 3xFP16."""
     from qflex_gb300 import FP16X3
-    assert autotune.variants(Context(-1, FP16X3)) == (0, 1, 2, 3)
+    assert autotune.variants(Context(-1, FP16X3)) == (0, 1, 2, 3, 4)
     assert autotune.variants(Context(-1, TF32X3)) == (0, 1)
     c = Context(-1, TF32X3)
     c.set_precision("fp16x3")
-    assert autotune.variants(c) == (0, 1, 2, 3)
+    assert autotune.variants(c) == (0, 1, 2, 3, 4)
