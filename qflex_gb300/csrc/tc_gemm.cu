@@ -744,6 +744,25 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
     for (int t = first; t < total && ok; t += stride) {
       int m0, n0, batch;
       tile_of(t, m0, n0, batch);
+      const int ncols = n - n0 - part * COLS;
+      // 3xFP16 scale exponents of the tile's store: the row's (unless A's
+      // blocks are applied per chunk) and, per 32-column piece, that of
+      // column j0 + lane. Loaded before the chunks are drained, so that
+      // their latency is hidden behind the drain.
+      int ea = 0, eb0 = 0, eb1 = 0;
+      bool fast = true;
+      if (KIND == KIND_FP16) {
+        ea = (a_blocks == 0 && m0 + row < m) ? exp_a[std::uint64_t(batch) * m + m0 + row] : 0;
+        const int* eb = exp_b + std::uint64_t(batch) * n + n0 + part * COLS;
+        eb0 = lane < ncols ? eb[lane] : 0;
+        eb1 = COLS > 32 && 32 + lane < ncols ? eb[32 + lane] : eb0;
+        // When every scale 2^-(ea + eb) of the warp's block is a normal
+        // float, each element takes one multiply by it (exact unless the
+        // result leaves the normal range, then rounded as ldexpf rounds).
+        const int lo = __reduce_min_sync(0xffffffffu, ea) + __reduce_min_sync(0xffffffffu, min(eb0, eb1));
+        const int hi = __reduce_max_sync(0xffffffffu, ea) + __reduce_max_sync(0xffffffffu, max(eb0, eb1));
+        fast = hi <= 126 && lo >= -127;
+      }
       float tre[COLS], tim[COLS];
 #pragma unroll
       for (int j = 0; j < COLS; ++j) tre[j] = tim[j] = 0.f;
@@ -790,23 +809,6 @@ __device__ __forceinline__ void cgemm_split_body(const CUtensorMap* map_a, const
       if (!ok) break;
       // The MMA issuer already works on the next tile. The warp's 32 x 64
       // block leaves in two 32 x 32 pieces through its staging area.
-      const int ncols = n - n0 - part * COLS;
-      // 3xFP16 scale exponents: the row's (unless A's blocks were applied
-      // per chunk) and, per piece, that of column j0 + lane.
-      int ea = 0, eb0 = 0, eb1 = 0;
-      bool fast = true;
-      if (KIND == KIND_FP16) {
-        ea = (a_blocks == 0 && m0 + row < m) ? exp_a[std::uint64_t(batch) * m + m0 + row] : 0;
-        const int* eb = exp_b + std::uint64_t(batch) * n + n0 + part * COLS;
-        eb0 = lane < ncols ? eb[lane] : 0;
-        eb1 = COLS > 32 && 32 + lane < ncols ? eb[32 + lane] : eb0;
-        // When every scale 2^-(ea + eb) of the warp's block is a normal
-        // float, each element takes one multiply by it (exact unless the
-        // result leaves the normal range, then rounded as ldexpf rounds).
-        const int lo = __reduce_min_sync(0xffffffffu, ea) + __reduce_min_sync(0xffffffffu, min(eb0, eb1));
-        const int hi = __reduce_max_sync(0xffffffffu, ea) + __reduce_max_sync(0xffffffffu, max(eb0, eb1));
-        fast = hi <= 126 && lo >= -127;
-      }
       // Output element (re, im) of column j of the piece: scaled by
       // 2^-(ea + eb_j), eb_j held by lane j. Otherwise by two powers of two
       // 2^e1 2^e2 (e1 + e2 = e, each clamped to the normal range): the first
