@@ -4,6 +4,8 @@
     python -m qflex_gb300.kernel_bench gemm --m 65536 --n 256 --k 256 --precision fp16x3 --batch 8
     python -m qflex_gb300.kernel_bench permute --bits 24 --seed 1
     python -m qflex_gb300.kernel_bench step --steps 3 --warmup 2 [--ordering supplied] [--chunk 2]
+    python -m qflex_gb300.kernel_bench ops --batch 8 --max-batch 4
+    python -m qflex_gb300.kernel_bench bias --precision fp16x3 --chunk 2
 
 Times launches with CUDA events on the context's stream (after warm-up) and
 prints one JSON line: average milliseconds per launch and the achieved
@@ -130,6 +132,44 @@ def bias(precision: str, chunk: int, debias: int, shapes) -> dict:
     return {"kernel": "bias", "precision": precision, "chunk": chunk, "debias": debias, "shapes": rows}
 
 
+def ops(precision: str, batch: int, max_batch: int, reps: int, warmup: int) -> dict:
+    """Device time of the benchmark step by operation, warm: `warmup` untimed
+    calls of evaluate_many over `batch` strings of the 7x7 (1+32+1)
+    workload, then `reps` profiled ones, in which every device op of the last
+    pass is bracketed by the engine's own CUDA events (captured graphs are
+    not used while profiling). Ops are grouped by kind and shape; times are
+    per pass (max_batch strings each) averaged over the profiled calls."""
+    import collections
+    torch, ctx, stream = _setup(precision)
+    from . import rqc
+    circuit, _, grid, initial, finals = rqc.workload("c3")
+    text = rqc.ordering_7x7_learned()
+    if max_batch > 0:
+        ctx.set_option("max_batch", max_batch)
+    strings = finals[:batch]
+    for _ in range(warmup):
+        ctx.evaluate_many(circuit, text, grid, initial, strings, 1 << 40)
+    names = ["permute", "cuda-core", "tensor-core", "skinny"]
+    ms, count, flop = collections.Counter(), collections.Counter(), collections.Counter()
+    ctx.set_profiling(True)
+    try:
+        for _ in range(reps):
+            ctx.evaluate_many(circuit, text, grid, initial, strings, 1 << 40)
+            for r in ctx.ops():
+                key = (names[int(r[0])], int(r[1]), int(r[2]), int(r[3]))
+                ms[key] += r[7] / reps
+                count[key] += 1.0 / reps
+                flop[key] += r[4] * r[6] / reps
+    finally:
+        ctx.set_profiling(False)
+    total = sum(ms.values())
+    rows = [{"op": k[0], "m": k[1], "n": k[2], "k": k[3], "launches": round(count[k], 1), "ms": v,
+             "share": v / total, "tflops": flop[k] / (v / 1e3) / 1e12 if flop[k] else None}
+            for k, v in sorted(ms.items(), key=lambda kv: -kv[1])]
+    return {"kernel": "ops", "precision": precision, "strings_per_pass": max_batch, "ms_per_pass": total,
+            "ops": rows}
+
+
 def main() -> None:
     p = argparse.ArgumentParser()
     sub = p.add_subparsers(dest="what", required=True)
@@ -157,9 +197,14 @@ def main() -> None:
     st.add_argument("--max-batch", type=int, default=4, help="strings per device pass (0: all that fit)")
     st.add_argument("--variant", type=int, default=-1, help="tensor-core kernel of every product (tc_variant)")
     st.add_argument("--debias", type=int, default=-1, help="tc_debias option (-1: the default)")
+    op = sub.add_parser("ops")
+    op.add_argument("--precision", default="fp16x3")
+    op.add_argument("--batch", type=int, default=8)
+    op.add_argument("--max-batch", type=int, default=4, help="strings per device pass")
     for s in (g, q):
         s.add_argument("--reps", type=int, default=5)
-    for s in (g, q, st):
+    op.add_argument("--reps", type=int, default=3)
+    for s in (g, q, st, op):
         s.add_argument("--warmup", type=int, default=2)
     g.add_argument("--chunk", type=int, default=0, help="TMEM chunk (0: the default)")
     a = p.parse_args()
@@ -167,6 +212,8 @@ def main() -> None:
         out = gemm(a.m, a.n, a.k, a.precision, a.reps, a.warmup, a.batch, a.variant, a.chunk)
     elif a.what == "step":
         out = step(a.precision, a.steps, a.warmup, a.batch, a.ordering, a.chunk, a.max_batch, a.variant, a.debias)
+    elif a.what == "ops":
+        out = ops(a.precision, a.batch, a.max_batch, a.reps, a.warmup)
     elif a.what == "bias":
         out = bias(a.precision, a.chunk, a.debias,
                    [(4096, 4096, 4096), (65536, 256, 256), (4096, 256, 4096), (16384, 1024, 64), (1024, 1024, 16)])
