@@ -191,13 +191,13 @@ __global__ void __launch_bounds__(256, 8) permute_kernel(const __grid_constant__
       // like their values, so one integer warp reduction finds it.
       const std::uint32_t mb = __reduce_max_sync(
           0xffffffffu, max(__float_as_uint(fabsf(v.x)), __float_as_uint(fabsf(v.y))));
-      // e with max * 2^e in [2^14, 2^15): a normal max of biased exponent E
-      // lies in [2^(E-127), 2^(E-126)); infinities and NaN keep e = 0.
-      const int E = int(mb >> 23);
+      // e with max * 2^e in [2^14, 2^15): a normal max of biased exponent be
+      // lies in [2^(be-127), 2^(be-126)); infinities and NaN keep e = 0.
+      const int be = int(mb >> 23);
       int e = 0;
-      if (E > 0 && E < 255) {
-        e = 141 - E;
-      } else if (E == 0 && mb != 0) {
+      if (be > 0 && be < 255) {
+        e = 141 - be;
+      } else if (be == 0 && mb != 0) {
         int ex;
         frexpf(__uint_as_float(mb), &ex);  // subnormal
         e = 15 - ex;
