@@ -519,7 +519,7 @@ def main():
             mma_rate = terms * achieved
             ai = 8.0 * m * n * k / (8.0 * (m * k + k * n + m * n))  # flop per byte, operands and result once
             line["roofline"] = {
-                "bound": "tensor", "kernel": f"cgemm_{args.precision} ({m},{n},{k}) x{pbatch} incl. B-plane split",
+                "bound": "tensor", "kernel": f"cgemm_{args.precision} ({m},{n},{k}) x{pbatch} incl. its operand splits",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "peak_source": src,
                 "mma_achieved": mma_rate, "mma_peak": mma_peak, "mma_frac": mma_rate / mma_peak,
