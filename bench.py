@@ -470,7 +470,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
             "config": dict(config(args), autotune=None if tuned is None else {
                 "variants": {sh: r["variant"] for sh, r in tuned["products"].items()},
-                "max_batch": tuned["max_batch"]}),
+                "max_batch": tuned["max_batch"], "ms_per_string": tuned.get("ms_per_string")}),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * 49 * B,
                     "d2h_bytes_per_step": 16 * B},
             "gpu_launches": int(st["launches"]) * args.steps,

@@ -85,9 +85,12 @@ def tune_products(ctx: Context, stream, shapes: Sequence[Tuple[int, int, int, in
 
 def tune_batch(ctx: Context, circuit: str, ordering: str, grid: str, initial: str,
                finals: Sequence[str], memory_limit: float, batches: Sequence[int] = (1, 2, 4, 8, 16),
-               reps: int = 1) -> dict:
+               reps: int = 3) -> dict:
     """Device time per amplitude of evaluate_many over `finals` for each
-    strings-per-pass limit; sets the fastest as "max_batch"."""
+    strings-per-pass limit, the best of `reps` calls after one untimed call;
+    sets the fastest as "max_batch". Neighbouring limits often differ by
+    1-2 %, about the spread of a single call at the power cap, hence the
+    repeats."""
     per_amp = {}
     for b in batches:
         if b > len(finals):
