@@ -83,14 +83,23 @@ def tune_products(ctx: Context, stream, shapes: Sequence[Tuple[int, int, int, in
     return out
 
 
+def choose_batch(per_amp: dict, tolerance: float = 0.01) -> int:
+    """The strings-per-pass limit to use, from device time per amplitude by
+    limit: the largest limit within `tolerance` of the fastest. Such near
+    ties are inside the spread of one call at the power cap, and a larger
+    pass makes fewer launches for the same work."""
+    best = min(per_amp.values())
+    return max(b for b, t in per_amp.items() if t <= best * (1.0 + tolerance))
+
+
 def tune_batch(ctx: Context, circuit: str, ordering: str, grid: str, initial: str,
                finals: Sequence[str], memory_limit: float, batches: Sequence[int] = (1, 2, 4, 8, 16),
                reps: int = 3) -> dict:
     """Device time per amplitude of evaluate_many over `finals` for each
     strings-per-pass limit, the best of `reps` calls after one untimed call;
-    sets the fastest as "max_batch". Neighbouring limits often differ by
-    1-2 %, about the spread of a single call at the power cap, hence the
-    repeats."""
+    sets choose_batch's pick as "max_batch". Neighbouring limits often differ
+    by 1-2 %, about the spread of a single call at the power cap, hence the
+    repeats and the tie rule."""
     per_amp = {}
     for b in batches:
         if b > len(finals):
@@ -104,7 +113,7 @@ def tune_batch(ctx: Context, circuit: str, ordering: str, grid: str, initial: st
         per_amp[b] = best / len(finals)
     if not per_amp:
         return {"max_batch": 0, "ms_per_string": {}}
-    choice = min(per_amp, key=per_amp.get)
+    choice = choose_batch(per_amp)
     ctx.set_option("max_batch", choice)
     return {"max_batch": choice, "ms_per_string": {str(b): t for b, t in per_amp.items()}}
 

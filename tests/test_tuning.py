@@ -69,6 +69,16 @@ def test_variants_graphs_and_batches_agree(built_lib, precision):
     assert ctx.stats()["batch"] == 4
 
 
+def test_choose_batch_prefers_larger_passes_on_near_ties():
+    """The strings-per-pass rule: the largest limit within 1 % of the
+    fastest, otherwise the fastest."""
+    assert autotune.choose_batch({1: 48.5, 2: 46.3, 4: 44.12, 8: 43.89}) == 8
+    assert autotune.choose_batch({1: 48.5, 2: 46.3, 4: 43.89, 8: 44.12}) == 8
+    assert autotune.choose_batch({1: 48.5, 2: 46.3, 4: 43.0, 8: 44.12}) == 4
+    assert autotune.choose_batch({4: 10.0}) == 4
+    assert autotune.choose_batch({1: 10.0, 2: 10.05}, tolerance=0.0) == 1
+
+
 @pytest.mark.gpu
 def test_autotune_sets_choices(built_lib, tmp_path):
     import torch
