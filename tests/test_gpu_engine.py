@@ -246,6 +246,30 @@ def test_simulate_drop_in(built_lib, ref_cases, capsys):
     assert "exceeds memory limit" in capsys.readouterr().err
 
 
+def test_simulate_as_the_cirq_adapter_calls_it(built_lib, ref_cases, tmp_path):
+    """The call pattern of the reference's Cirq adapter
+    (qflexcirq/interface/qflex_simulator.py:44-60): circuit, ordering and
+    grid written to files whose paths go in the *_filename keys, no initial
+    state, one simulate() per final state, amplitudes taken as complex(amp[1])
+    in the order returned. cirq itself is not installed, so the adapter's own
+    code does not run here."""
+    case = ref_cases["simple"]
+    paths = {}
+    for name in ("circuit", "ordering", "grid"):
+        paths[name] = tmp_path / f"{name}.txt"
+        paths[name].write_text(case[name])
+    amplitudes = []
+    for bitstring in ("1100x", "0000x"):
+        options = {"circuit_filename": str(paths["circuit"]), "ordering_filename": str(paths["ordering"]),
+                   "grid_filename": str(paths["grid"]), "final_state": bitstring}
+        amplitudes.append([complex(amp[1]) for amp in simulate(options)])
+    assert len(amplitudes[0]) == len(amplitudes[1]) == 2
+    # The reference's known answer for 1100x from the all-zero initial state
+    # (tests/src/evaluate_circuit_test.cpp:203-206).
+    assert abs(amplitudes[0][0] - (0.10669 + 0.04419j)) < 2e-5
+    assert abs(amplitudes[0][1] - (-0.01831 - 0.25758j)) < 2e-5
+
+
 @pytest.mark.parametrize("precision", ["fp32", "fp16x3"])
 def test_open_terminals_match_projection_and_fp64(built_lib, precision):
     """Terminal cuts as open indices give the amplitudes of the reference's
