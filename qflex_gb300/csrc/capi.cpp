@@ -42,6 +42,9 @@ int guarded(qflex_gb300_context* ctx, F&& f) {
   } catch (const std::exception& e) {
     ctx->error = e.what();
     return QFLEX_GB300_ERR_INPUT;
+  } catch (...) {  // nothing may cross the C ABI
+    ctx->error = "ERROR (qflex_gb300) --> unknown exception";
+    return QFLEX_GB300_ERR_INPUT;
   }
 }
 
@@ -298,13 +301,17 @@ int qflex_gb300_set_profiling(qflex_gb300_context* ctx, int on) {
 
 size_t qflex_gb300_last_ops(const qflex_gb300_context* ctx, double* out, size_t cap) {
   if (!ctx || !ctx->engine) return 0;
-  const auto ops = ctx->engine->last_ops();
-  for (size_t i = 0; i < ops.size() && i < cap && out; ++i) {
-    const auto& r = ops[i];
-    const double row[8] = {double(r.kind), r.m, r.n, r.k, r.flop, r.bytes, r.batch, r.ms};
-    std::memcpy(out + 8 * i, row, sizeof(row));
+  try {  // the op list is built on the host: nothing may cross the C ABI
+    const auto ops = ctx->engine->last_ops();
+    for (size_t i = 0; i < ops.size() && i < cap && out; ++i) {
+      const auto& r = ops[i];
+      const double row[8] = {double(r.kind), r.m, r.n, r.k, r.flop, r.bytes, r.batch, r.ms};
+      std::memcpy(out + 8 * i, row, sizeof(row));
+    }
+    return ops.size();
+  } catch (...) {
+    return 0;
   }
-  return ops.size();
 }
 
 int qflex_gb300_permute(qflex_gb300_context* ctx, const void* src, void* dst, size_t rank,
@@ -409,6 +416,9 @@ int parse_guarded(char* err, std::size_t err_len, F&& f) {
   } catch (const std::exception& e) {
     put(e.what());
     return QFLEX_GB300_ERR_INPUT;
+  } catch (...) {  // nothing may cross the C ABI
+    put("ERROR (qflex_gb300) --> unknown exception");
+    return QFLEX_GB300_ERR_INPUT;
   }
 }
 
@@ -419,8 +429,11 @@ extern "C" {
 int qflex_gb300_circuit_load(const char* text, qflex_gb300_circuit** out, char* err, size_t err_len) {
   if (!out) return QFLEX_GB300_ERR_ARG;
   *out = nullptr;
-  auto c = std::make_unique<qflex_gb300_circuit>();
-  const int rc = parse_guarded(err, err_len, [&] { c->circuit.load(text ? text : ""); });
+  std::unique_ptr<qflex_gb300_circuit> c;
+  const int rc = parse_guarded(err, err_len, [&] {
+    c = std::make_unique<qflex_gb300_circuit>();
+    c->circuit.load(text ? text : "");
+  });
   if (rc == QFLEX_GB300_OK) *out = c.release();
   return rc;
 }
