@@ -26,6 +26,7 @@
 #include <cstdio>
 #include <fstream>
 #include <iostream>
+#include <memory>
 #include <sstream>
 #include <string>
 #include <utility>
@@ -99,8 +100,13 @@ struct QflexCircuit {
   void parse(const std::string& text) {
     clear();
     char err[4096];
-    qflex_gb300_circuit* c = nullptr;
-    if (qflex_gb300_circuit_load(text.c_str(), &c, err, sizeof(err)) != QFLEX_GB300_OK) throw std::string(err);
+    qflex_gb300_circuit* raw_handle = nullptr;
+    if (qflex_gb300_circuit_load(text.c_str(), &raw_handle, err, sizeof(err)) != QFLEX_GB300_OK)
+      throw std::string(err);
+    // Freed however this function is left.
+    const std::unique_ptr<qflex_gb300_circuit, void (*)(qflex_gb300_circuit*)> handle(raw_handle,
+                                                                                     qflex_gb300_circuit_free);
+    const qflex_gb300_circuit* c = handle.get();
     num_active_qubits = qflex_gb300_circuit_num_active_qubits(c);
     depth = qflex_gb300_circuit_depth(c);
     const std::size_t n = qflex_gb300_circuit_gate_count(c);
@@ -110,14 +116,13 @@ struct QflexCircuit {
       double params[8];
       qflex_gb300_circuit_gate(c, i, &name, &raw, &cycle, qubits, 8, &nq, params, 8, &np);
       QflexGate g;
-      g.name = name;
-      g.raw = raw;
+      g.name = name ? name : "";
+      g.raw = raw ? raw : "";
       g.cycle = cycle;
       g.qubits.assign(qubits, qubits + (nq < 8 ? nq : 8));
       g.params.assign(params, params + (np < 8 ? np : 8));
       gates.push_back(std::move(g));
     }
-    qflex_gb300_circuit_free(c);
   }
 };
 
