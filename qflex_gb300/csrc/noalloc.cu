@@ -97,6 +97,9 @@ extern "C" int qflex_gb300_multiply_skinny_noalloc(const void* A, const void* B,
   } catch (const std::string& msg) {
     put_error(err, err_len, msg.c_str());
     return QFLEX_GB300_ERR_CUDA;
+  } catch (...) {  // nothing may cross the C ABI
+    put_error(err, err_len, "unknown exception");
+    return QFLEX_GB300_ERR_CUDA;
   }
   return QFLEX_GB300_OK;
 }
