@@ -24,7 +24,7 @@ host between steps, never inside a kernel.
 from __future__ import annotations
 
 import datetime
-import pickle
+import json
 import re
 from typing import Callable, List, Optional, Sequence, Tuple
 
@@ -116,13 +116,29 @@ def _wait(store, keys: List[str], timeout_s: float) -> List[str]:
         return missing
 
 
-def exchange(store, tag: str, rank: int, world: int, payload, error: Optional[str],
-             timeout_s: float) -> list:
-    """Publishes this rank's payload (or error), waits for every rank and
-    returns the payloads in rank order. Raises ShardError on every rank if
+def encode_result(result: Result) -> bytes:
+    """A rank's (state, amplitude) list as JSON: [[state, re, im], ...].
+    JSON, unlike pickle, runs nothing when read, and Python writes floats
+    with repr, so every double round-trips exactly."""
+    return json.dumps([[str(st), float(complex(a).real), float(complex(a).imag)] for st, a in result]).encode()
+
+
+def decode_result(data: bytes) -> Result:
+    rows = json.loads(data.decode())
+    if not isinstance(rows, list) or not all(
+            isinstance(r, list) and len(r) == 3 and isinstance(r[0], str) and all(
+                isinstance(x, (int, float)) for x in r[1:]) for r in rows):
+        raise ShardError("malformed result payload")
+    return [(st, complex(re_, im)) for st, re_, im in rows]
+
+
+def exchange(store, tag: str, rank: int, world: int, payload: Result, error: Optional[str],
+             timeout_s: float) -> List[Result]:
+    """Publishes this rank's results (or error), waits for every rank and
+    returns the results in rank order. Raises ShardError on every rank if
     any rank failed or did not report in time."""
     if error is None:
-        store.set(f"{tag}/data/{rank}", pickle.dumps(payload))
+        store.set(f"{tag}/data/{rank}", encode_result(payload))
         store.set(f"{tag}/status/{rank}", b"ok")
     else:
         store.set(f"{tag}/status/{rank}", b"error:" + error.encode())
@@ -138,7 +154,7 @@ def exchange(store, tag: str, rank: int, world: int, payload, error: Optional[st
             failed.append(f"rank {r}: {st[len(b'error:'):].decode(errors='replace')}")
     if failed:
         raise ShardError("; ".join(failed))
-    return [pickle.loads(store.get(f"{tag}/data/{r}")) for r in range(world)]
+    return [decode_result(store.get(f"{tag}/data/{r}")) for r in range(world)]
 
 
 def evaluate_sharded(evaluate: Evaluate, circuit: str, ordering: str, grid: str, initial: str,

@@ -147,3 +147,24 @@ def test_rank_that_never_reports_times_out():
     assert out[1][0] == "vanished"
     status, msg = out[0]
     assert status == "error" and "did not report" in msg and "[1]" in msg
+
+
+def test_result_codec_round_trips_doubles_exactly():
+    """Ranks exchange results as JSON (nothing runs when a payload is read);
+    every double comes back bit for bit, NaN included (planning-only
+    contexts return NaN amplitudes), and a malformed payload is refused."""
+    import math
+    import struct
+
+    vals = [0.1 + 0.2j, complex(-1e-300, 5e-324), complex(1.7976931348623157e308, -0.0),
+            complex(float("nan"), 1.0), 0j]
+    res = [(f"{i:05b}", v) for i, v in enumerate(vals)]
+    back = shards.decode_result(shards.encode_result(res))
+    assert [s for s, _ in back] == [s for s, _ in res]
+    bits = lambda x: struct.pack("<d", x)  # noqa: E731
+    for (_, a), (_, b) in zip(res, back):
+        for x, y in ((a.real, b.real), (a.imag, b.imag)):
+            assert (math.isnan(x) and math.isnan(y)) or bits(x) == bits(y)
+    for bad in (b'{"a": 1}', b'[["00", "x", 1.0]]', b'[["00", 1.0]]'):
+        with pytest.raises(shards.ShardError):
+            shards.decode_result(bad)
