@@ -162,3 +162,66 @@ def test_open_terminals_fall_back_to_projection(built_lib):
     b = p1.evaluate(c, partial, g, ini, finals[0], 1 << 40)
     assert [s for s, _ in a] == [s for s, _ in b] and len(a) == 2
     assert p0.stats()["n_ops"] == p1.stats()["n_ops"]
+
+
+def _sweep(I, J, off, order):
+    """A one-patch sweep over the active qubits: row by row, column by
+    column, or row by row snaking."""
+    cells = []
+    if order == "cols":
+        cells = [(i, j) for j in range(J) for i in range(I)]
+    else:
+        for i in range(I):
+            row = [(i, j) for j in range(J)]
+            cells += row[::-1] if order == "snake" and i % 2 else row
+    return [i * J + j for i, j in cells if (i, j) not in off]
+
+
+@pytest.mark.parametrize("seed", range(10))
+def test_random_plans_match_oracle(plan_ctx, seed):
+    """Seeded random grids, depths, sweep orders, two-qubit cuts (full or
+    partial value lists) and terminal cuts: the planner's output states,
+    mutated input states and product sequence equal the oracle's (the
+    products after the oracle's flatten phase, which the engine runs as
+    flatten_kernel instead)."""
+    import random
+
+    rng = random.Random(seed)
+    I, J = rng.choice([(3, 3), (3, 4), (4, 3), (2, 5)])
+    off = {(rng.randrange(I), rng.randrange(J))} if seed % 3 == 2 else set()
+    depth = rng.choice([8, 12])
+    circuit = rqc.random_circuit(I, J, depth, seed, off)
+    grid = rqc.grid_text(I, J, off)
+    seq = _sweep(I, J, off, rng.choice(["rows", "cols", "snake"]))
+    n_term = rng.choice([0, 0, 1, 2])
+    term = seq[len(seq) - n_term:] if n_term else []
+    lines = []
+    if seed % 2:
+        # A cut on a bond between horizontal neighbours, placed before any
+        # expansion of their tensors (a cut must precede them).
+        pairs = [(i * J + j, i * J + j + 1) for i in range(I) for j in range(J - 1)
+                 if (i, j) not in off and (i, j + 1) not in off
+                 and i * J + j not in term and i * J + j + 1 not in term]
+        q1, q2 = rng.choice(pairs)
+        lines.append(f"cut ({rng.choice(['0,1', '1'])}) {q1} {q2}")
+    lines += [f"expand a {q}" for q in seq[:len(seq) - n_term]]
+    if term:
+        lines += [f"cut () {q}" for q in term] + [f"expand b {q}" for q in term] + ["merge a b"]
+    ordering = "\n".join(lines) + "\n"
+    active = [i * J + j for i in range(I) for j in range(J) if (i, j) not in off]
+    final = list(rqc.random_bitstrings(len(active), 1, seed + 100)[0])
+    for q in term:
+        final[active.index(q)] = "x"
+    final = "".join(final)
+    initial = rqc.random_bitstrings(len(active), 1, seed + 200)[0]
+
+    got = plan_ctx.evaluate(circuit, ordering, grid, initial, final, 1 << 40)
+    log = []
+    inp = qo.Input(qo.Circuit.loads(circuit), qo.load_ordering(ordering), qo.Grid.loads(grid), initial, final)
+    want = qo.evaluate_circuit(inp, np.complex64, float(1 << 40), log=log)
+    assert [s for s, _ in got] == [s for s, _ in want]
+    assert len(got) == 2 ** n_term
+    assert plan_ctx.initial_state() == inp.initial_state
+    assert plan_ctx.final_state() == inp.final_state
+    gemms = plan_ctx.gemms()
+    assert gemms and [tuple(x[1:]) for x in log[len(log) - len(gemms):]] == gemms
