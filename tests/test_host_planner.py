@@ -177,13 +177,13 @@ def _sweep(I, J, off, order):
     return [i * J + j for i, j in cells if (i, j) not in off]
 
 
-@pytest.mark.parametrize("seed", range(10))
+@pytest.mark.parametrize("seed", range(16))
 def test_random_plans_match_oracle(plan_ctx, seed):
-    """Seeded random grids, depths, sweep orders, two-qubit cuts (full or
-    partial value lists) and terminal cuts: the planner's output states,
-    mutated input states and product sequence equal the oracle's (the
-    products after the oracle's flatten phase, which the engine runs as
-    flatten_kernel instead)."""
+    """Seeded random grids, depths, sweep orders, two-patch sweeps with a
+    merge, two-qubit cuts (full or partial value lists) and terminal cuts:
+    the planner's output states, mutated input states and product sequence
+    equal the oracle's (the products after the oracle's flatten phase,
+    which the engine runs as flatten_kernel instead)."""
     import random
 
     rng = random.Random(seed)
@@ -204,9 +204,18 @@ def test_random_plans_match_oracle(plan_ctx, seed):
                  and i * J + j not in term and i * J + j + 1 not in term]
         q1, q2 = rng.choice(pairs)
         lines.append(f"cut ({rng.choice(['0,1', '1'])}) {q1} {q2}")
-    lines += [f"expand a {q}" for q in seq[:len(seq) - n_term]]
+    main = seq[:len(seq) - n_term]
+    if seed % 4 >= 2:
+        # Two patches over the sweep's halves, the first merged into the second.
+        half = len(main) // 2
+        lines += [f"expand a {q}" for q in main[:half]] + [f"expand m {q}" for q in main[half:]]
+        lines.append("merge a m")
+        last = "m"
+    else:
+        lines += [f"expand a {q}" for q in main]
+        last = "a"
     if term:
-        lines += [f"cut () {q}" for q in term] + [f"expand b {q}" for q in term] + ["merge a b"]
+        lines += [f"cut () {q}" for q in term] + [f"expand t {q}" for q in term] + [f"merge {last} t"]
     ordering = "\n".join(lines) + "\n"
     active = [i * J + j for i in range(I) for j in range(J) if (i, j) not in off]
     final = list(rqc.random_bitstrings(len(active), 1, seed + 100)[0])
