@@ -57,7 +57,14 @@ std::vector<Op> parse_ordering(const Ordering& ord, const Grid& grid) {
     if (op == "expand") {
       Op e{Op::EXPAND};
       long idx = 0;
-      ss >> e.patch >> idx;
+      ss >> e.patch >> std::ws;
+      // A line that ends before the index leaves the reference's index
+      // uninitialized (its extraction fails at end of stream and stores
+      // nothing, src/contraction_utils.cpp:390-396): refused here. A token
+      // that is not a number reads as 0 there (a failed conversion stores
+      // 0) and reads as 0 here.
+      if (ss.eof()) throw error("Expand needs a patch name and a qubit index.");
+      ss >> idx;
       check(idx);
       e.tensor = coords(idx);
       if (grid.is_off(e.tensor.first, e.tensor.second))
@@ -195,8 +202,16 @@ std::vector<std::complex<T>> one_qubit_gate(const Gate& g) {
     return {std::conj(phase), C(0), C(0), phase};
   }
   auto t = table_gate<T>(g.name);
-  if (t.size() != 4) throw QFX_ERR("Invalid gate name provided: ", g.name);
-  return t;
+  if (t.size() == 4) return t;
+  // The reference's gate table also holds the full cz and cx (16 entries,
+  // src/read_circuit.cpp:61-79). Used on one qubit, they and the two-qubit
+  // halves (8 entries) pass its name check, and the one-qubit tensor
+  // (4 entries) refuses their data (src/read_circuit.cpp:419-427,
+  // src/tensor.cpp:170-180).
+  const std::size_t entries = (g.name == "cz" || g.name == "cx") ? 16 : t.size();
+  if (entries == 0) throw QFX_ERR("Invalid gate name provided: ", g.name);
+  throw QFX_ERR("Failed to call Tensor(). Error:\n\t[The vector data size: ", entries,
+                ", has to match the size of the Tensor: 4]");
 }
 
 // fSim(theta, phi) split into two identical (input, virtual[4], output)

@@ -234,3 +234,41 @@ def test_random_plans_match_oracle(plan_ctx, seed):
     assert plan_ctx.final_state() == inp.final_state
     gemms = plan_ctx.gemms()
     assert gemms and [tuple(x[1:]) for x in log[len(log) - len(gemms):]] == gemms
+
+
+def _input_error_cases():
+    import json
+
+    from tests.conftest import ROOT
+    return json.loads((ROOT / "tests" / "golden" / "input_errors.json").read_text())
+
+
+def _squash(text):
+    return " ".join(text.split())
+
+
+@pytest.mark.parametrize("case", _input_error_cases()["cases"], ids=lambda c: c["name"])
+def test_malformed_inputs_match_reference(plan_ctx, case):
+    """Seeded malformed circuits, orderings, grids and states, and a few valid
+    ones, against the unmodified reference's outcome
+    (tests/golden/input_errors.json, made by make_input_errors.py): the same
+    output states, or an error whose text contains the reference's innermost
+    message (whitespace compared loosely: the reference's driver prints its
+    multi-line messages on one line)."""
+    run = lambda: plan_ctx.evaluate(case["circuit"], case["ordering"], case["grid"],  # noqa: E731
+                                    case["initial"], case["final"], 1 << 30)
+    if "error" in case:
+        with pytest.raises(QflexGb300Error) as e:
+            run()
+        assert _squash(case["error"]) in _squash(str(e.value)), str(e.value)
+    else:
+        assert [s for s, _ in run()] == case["states"]
+
+
+@pytest.mark.parametrize("case", _input_error_cases()["reference_undefined"], ids=lambda c: c["name"])
+def test_inputs_undefined_in_the_reference_are_refused(plan_ctx, case):
+    """Where the reference's behaviour is undefined (the fixture says why),
+    the engine refuses the input with an error instead of computing."""
+    with pytest.raises(QflexGb300Error):
+        plan_ctx.evaluate(case["circuit"], case["ordering"], case["grid"], case["initial"], case["final"],
+                          1 << 30)
