@@ -6,7 +6,7 @@ Every case records the reference's outcome: the output states of a valid
 input, or the innermost message of the error it throws (the text after the
 last "--> " of its nested "Failed to call X()" chain, which names the
 reference's own source paths and is not kept). Inputs on which the reference
-itself crashes instead of throwing are listed by name only; those on which its
+itself crashes instead of throwing are recorded apart; those on which its
 behaviour is undefined (UNDEFINED below) are recorded apart, with the reason,
 and are no parity target.
 
@@ -163,12 +163,12 @@ def main() -> None:
         inputs.append(("states: " + what, CIRCUIT, TERMINAL_ORDERING, GRID, ini, fin))
     cases, undefined, crashed = [], [], []
     for name, c, o, g, ini, fin in inputs:
+        rec = {"name": name, "circuit": c, "ordering": o, "grid": g, "initial": ini, "final": fin}
         try:
             r = run_ref(c, o, g, ini, fin, "1GB")
         except RuntimeError:
-            crashed.append(name)
+            crashed.append(rec)
             continue
-        rec = {"name": name, "circuit": c, "ordering": o, "grid": g, "initial": ini, "final": fin}
         if "error" in r:
             rec["error"] = innermost(r["error"])
         else:
@@ -180,7 +180,7 @@ def main() -> None:
     OUT.write_text(json.dumps({"cases": cases, "reference_undefined": undefined, "reference_crashed": crashed},
                               indent=1) + "\n")
     print(f"{len(cases)} cases ({sum('error' in c for c in cases)} errors), {len(undefined)} undefined, "
-          f"reference crashed on {crashed}")
+          f"reference crashed on {[c['name'] for c in crashed]}")
 
 
 if __name__ == "__main__":

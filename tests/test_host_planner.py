@@ -272,3 +272,12 @@ def test_inputs_undefined_in_the_reference_are_refused(plan_ctx, case):
     with pytest.raises(QflexGb300Error):
         plan_ctx.evaluate(case["circuit"], case["ordering"], case["grid"], case["initial"], case["final"],
                           1 << 30)
+
+
+@pytest.mark.parametrize("case", _input_error_cases()["reference_crashed"], ids=lambda c: c["name"])
+def test_inputs_that_crash_the_reference_are_refused(plan_ctx, case):
+    """Inputs on which the reference crashes instead of throwing are refused
+    with an error by the engine."""
+    with pytest.raises(QflexGb300Error):
+        plan_ctx.evaluate(case["circuit"], case["ordering"], case["grid"], case["initial"], case["final"],
+                          1 << 30)
