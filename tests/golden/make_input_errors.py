@@ -125,6 +125,26 @@ def ordering_mutations(rng: random.Random):
     return out
 
 
+def format_variants():
+    """Formatting that real input files carry: (what, circuit, ordering, grid)."""
+    crlf = lambda t: t.replace("\n", "\r\n")  # noqa: E731
+    return [
+        ("CRLF line endings in the circuit", crlf(CIRCUIT), ORDERING, GRID),
+        ("CRLF line endings in the ordering", CIRCUIT, crlf(ORDERING), GRID),
+        ("CRLF line endings in the grid", CIRCUIT, ORDERING, crlf(GRID)),
+        ("tabs between circuit tokens", CIRCUIT.replace("1 cz 0 1", "1\tcz\t0\t1"), ORDERING, GRID),
+        ("leading spaces in the circuit", CIRCUIT.replace("3 t 4", "   3 t 4"), ORDERING, GRID),
+        ("trailing spaces in the circuit", CIRCUIT.replace("3 t 4", "3 t 4   "), ORDERING, GRID),
+        ("spaces inside gate parameters", CIRCUIT.replace("fsim(0.25, 0.1)", "fsim( 0.25 , 0.1 )"), ORDERING, GRID),
+        ("comment lines in the ordering", CIRCUIT, "# sweep\n" + ORDERING.replace("expand a 3", "# here\nexpand a 3"),
+         GRID),
+        ("blank lines in the ordering", CIRCUIT, ORDERING.replace("expand a 3\n", "expand a 3\n\n"), GRID),
+        ("trailing blank lines in the grid", CIRCUIT, ORDERING, GRID + "\n\n"),
+        ("extra spaces in the grid", CIRCUIT, ORDERING, "1  1 1\n 1 1 1\n"),
+        ("tabs in the ordering", CIRCUIT, ORDERING.replace("expand a 3", "expand\ta\t3"), GRID),
+    ]
+
+
 def grid_mutations():
     return [
         ("ragged grid", "1 1 1\n1 1\n"),
@@ -157,6 +177,8 @@ def main() -> None:
         inputs.append(("ordering: " + what, CIRCUIT, o, GRID, "", ""))
     for what, g in grid_mutations():
         inputs.append(("grid: " + what, CIRCUIT, ORDERING, g, "", ""))
+    for what, c, o, g in format_variants():
+        inputs.append(("format: " + what, c, o, g, "", ""))
     for what, ini, fin in state_mutations():
         inputs.append(("states: " + what, CIRCUIT, ORDERING, GRID, ini, fin))
     for what, ini, fin in (("terminal states", "", "0101xx"), ("terminal x in a cut-free qubit", "", "x101xx")):
