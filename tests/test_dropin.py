@@ -89,3 +89,51 @@ def test_cli_known_answer_and_errors(built_lib, tmp_path, ref_cases):
                          timeout=600)
     assert out.returncode == 2 and out.stdout == ""
     assert "Failed to call EvaluateCircuit()" in out.stderr and "exceeds memory limit" in out.stderr
+
+
+def test_simulate_option_handling_matches_pybind(built_lib, ref_cases, tmp_path, capsys):
+    """qflex.simulate's option handling (src/pybind_main.cpp:26-138), on a
+    planning-only context: every malformed option prints the reference's
+    message and returns []; the data keys load in the order grid, circuit,
+    ordering, so the first bad one is the one reported; the memory limit is
+    global state as there; a valid call returns the reference's output
+    states."""
+    from qflex_gb300 import Context
+    from qflex_gb300.qflex import simulate
+
+    ctx = Context(-1)
+    case = ref_cases["simple"]
+    base = {"circuit": case["circuit"].splitlines(), "ordering": case["ordering"].splitlines(),
+            "grid": case["grid"].splitlines(), "initial_state": "00000", "final_state": "1100x"}
+
+    out = simulate(dict(base), context=ctx)
+    assert [s for s, _ in out] == ["11000", "11001"]
+    assert [s for s, _ in simulate(dict(base, memory_limit="16GB"), context=ctx)] == ["11000", "11001"]
+    capsys.readouterr()
+
+    def message(options):
+        assert simulate(options, context=ctx) == []
+        return capsys.readouterr().err
+
+    assert "'circuit' must be a list of strings." in message(dict(base, circuit=5))
+    no_grid = {k: v for k, v in base.items() if k != "grid"}
+    assert "'grid_filename' must be a string." in message(dict(no_grid, grid_filename=3))
+    # grid loads first: with both malformed, the grid is reported
+    assert "'grid' must be a list of strings." in message(dict(base, grid=1, circuit=5))
+    assert "Not yet supported" in message(dict(base, final_states=["1100x", "0000x"]))
+    assert "states must be strings." in message(dict(base, initial_states=["00000", 7]))
+    assert "final_states must be a list of strings." in message(dict(base, final_states=7))
+    assert "states must be strings." in message(dict(base, final_state=7))
+    assert "'memory_limit' must be positive." in message(dict(base, memory_limit=0))
+    no_circuit = {k: v for k, v in base.items() if k != "circuit"}
+    missing = tmp_path / "missing.txt"
+    assert f"Cannot open circuit file {missing}." in message(dict(no_circuit, circuit_filename=str(missing)))
+    assert "exceeds memory limit" in message(dict(base, memory_limit=64))
+    # A memory_limit of another type is not an error there (the message is
+    # built but not thrown): the limit is global state and keeps the
+    # previous call's value, here 64 bytes, then 16 GB.
+    assert "exceeds memory limit" in message(dict(base, memory_limit=1.5))
+    simulate(dict(base, memory_limit="16GB"), context=ctx)
+    assert [s for s, _ in simulate(dict(base, memory_limit=1.5), context=ctx)] == ["11000", "11001"]
+    # Without the key the limit returns to the 1 GiB default.
+    assert [s for s, _ in simulate(dict(base), context=ctx)] == ["11000", "11001"]
