@@ -137,3 +137,22 @@ def test_simulate_option_handling_matches_pybind(built_lib, ref_cases, tmp_path,
     assert [s for s, _ in simulate(dict(base, memory_limit=1.5), context=ctx)] == ["11000", "11001"]
     # Without the key the limit returns to the 1 GiB default.
     assert [s for s, _ in simulate(dict(base), context=ctx)] == ["11000", "11001"]
+
+
+def test_cli_argument_errors(built_lib, tmp_path):
+    """The CLI's failures before any evaluation (no GPU needed): missing
+    arguments print the usage with exit code 1; an unknown precision and an
+    unreadable input file are error messages, exit code 2, as the reference's
+    main.cpp returns for a thrown message (src/main.cpp:148-155)."""
+    assert CLI.exists()
+    usage = subprocess.run([str(CLI)], capture_output=True, text=True, timeout=60)
+    assert usage.returncode == 1 and "qflex" in usage.stderr.lower()
+    for name in ("c.txt", "o.txt", "g.txt"):
+        (tmp_path / name).write_text("1 1\n" if name == "g.txt" else "")
+    args = ["-c", str(tmp_path / "c.txt"), "-o", str(tmp_path / "o.txt"), "-g", str(tmp_path / "g.txt")]
+    bad = subprocess.run([str(CLI), *args, "--precision=fp8"], capture_output=True, text=True, timeout=60)
+    assert bad.returncode == 2 and "Unknown precision fp8" in bad.stderr
+    missing = tmp_path / "none.txt"
+    args[1] = str(missing)
+    gone = subprocess.run([str(CLI), *args], capture_output=True, text=True, timeout=60)
+    assert gone.returncode == 2 and f"Cannot open circuit file {missing}" in gone.stderr
